@@ -1,0 +1,295 @@
+#!/usr/bin/env python3
+"""Benchmark of the TWMC trajectory engine on the 2-D 64 x 64 workload.
+
+Workload (the headline configuration): 2-D square lattice 64 x 64, PBC,
+J = 1, U = 0.2, gamma = 1, omega_i = -0.5 + N(0, 0.2^2) site disorder drawn
+per trajectory, F = 2.0, vacuum Wigner start (beta_init = 0, sigma = 0.5),
+dt = 0.002, frames every 0.5 (250 steps), 16384 trajectories, complex64
+state and FFT, FP64 ensemble moments. Synthetic inputs, seeded.
+
+One bench step = one frame of the whole batch: 250 Euler-Maruyama steps of
+all 16384 trajectories (on-chip FFT hopping) plus the FP64 reduction of the
+frame's moments. The state (512 MB) is larger than L2, so every launch
+streams it from HBM.
+
+Metric: site-updates/s (sites x steps x trajectories per second).
+
+  python bench.py [--gpus N --steps K --warmup W]          this engine
+  python bench.py --impl reference [...]                   the CPU arm
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+NX = NY = 64
+NTRAJ = 16384
+DT = 0.002
+FRAME_STEPS = 250
+T_END = 100.0
+FLOPS_PER_SITE_UPDATE = 10 * 12 + 26  # 10 log2(N) + 26 for N = 4096
+BYTES_PER_SITE_UPDATE_HBM = 16.0 / FRAME_STEPS  # state read + written once per launch (complex64)
+METRIC = "site-updates/s"
+CONFIG = {
+    "workload": "2D 64x64 PBC, 16384 trajectories, J=1 U=0.2 gamma=1 omega=-0.5+N(0,0.04) F=2 dt=0.002, "
+                "frame = 250 steps (+FP64 moments), complex64 state/FFT",
+    "lattice": [NX, NY], "trajectories": NTRAJ, "dt": DT, "steps_per_bench_step": FRAME_STEPS,
+    "l2": "state 512 MB > L2, re-read from HBM every launch",
+}
+
+
+def env_rank():
+    return (int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")),
+            int(os.environ.get("LOCAL_RANK", "0")))
+
+
+def clock_sampler_start(path):
+    q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    try:
+        f = open(path, "w")
+        return subprocess.Popen(["nvidia-smi", f"--query-gpu={q}", "--format=csv,noheader,nounits", "-lms", "200"],
+                                stdout=f, stderr=subprocess.DEVNULL), f
+    except Exception:
+        return None, None
+
+
+def clock_sampler_stop(proc, f, path, gpu_index):
+    if proc is None:
+        return None
+    proc.terminate()
+    try:
+        proc.wait(timeout=5)
+    except Exception:
+        proc.kill()
+    f.close()
+    sm, smax, reasons = [], 0.0, set()
+    names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+    for line in open(path):
+        parts = [p.strip() for p in line.split(",")]
+        if len(parts) < 9 or not parts[0].isdigit() or int(parts[0]) != gpu_index:
+            continue
+        try:
+            sm.append(float(parts[1]))
+            smax = max(smax, float(parts[2]))
+        except ValueError:
+            continue
+        for nm, v in zip(names, parts[5:9]):
+            if v.lower().startswith("active"):
+                reasons.add(nm)
+    if not sm:
+        return None
+    return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        return {}
+
+
+def ncu_traffic():
+    """DRAM bytes per step-kernel launch from the committed ncu summary (or None)."""
+    try:
+        d = json.load(open(os.path.join(ROOT, "profiles", "square_fft_kernel_64x64.json")))
+        return d.get("dram_bytes_per_launch_full_size")
+    except Exception:
+        return None
+
+
+def make_system(twmc, hop=None):
+    return twmc.System(nx=NX, ny=NY, J=1.0, gamma=1.0, dt=DT, frame_steps=FRAME_STEPS,
+                       omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=0.2, F=2.0, beta_init=0.0,
+                       beta_init_sigma=0.5, precision=twmc.PREC_F32,
+                       hop=twmc.HOP_FFT if hop is None else hop, n_moment_blocks=32)
+
+
+def cpu_baseline(target_s=12.0, threads=None):
+    """Oracle port (FP64 restatement, radix-2 FFT, not FFTW) on the host cores:
+    a bounded sample of the same workload (trajectories x 250 steps of 64 x 64)."""
+    import numpy as np
+    from oracle import loader as orc
+
+    lib = orc.load(fast=True)
+    threads = threads or os.cpu_count() or 1
+    n = NX * NY
+    rng = np.random.default_rng(0)
+    omega = np.ascontiguousarray(-0.5 + 0.2 * rng.normal(size=n) + 0j)
+    U = np.full(n, 0.2 + 0j)
+    F = np.full(n, 2.0 + 0j)
+    b0 = np.ascontiguousarray(0.5 * (rng.normal(size=n) + 1j * rng.normal(size=n)))
+
+    def run(ntraj, steps):
+        t0 = time.perf_counter()
+        done = lib.orc_base_run_batch(NX, NY, 1.0, 1.0, DT, 0.0, (steps - 0.5) * DT, steps, 2, omega.ctypes.data,
+                                      U.ctypes.data, F.ctypes.data, b0.ctypes.data, ntraj, 1, threads, None)
+        return done, time.perf_counter() - t0
+
+    steps = 25
+    _, t1 = run(threads, steps)  # calibration: one trajectory per thread
+    per_round = max(t1, 1e-3)
+    rounds = max(1, int(target_s / per_round))
+    ntraj = threads * rounds
+    done, el = run(ntraj, steps)
+    su = float(done) * steps * n
+    return {"value": su / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{done} trajectories x {steps} steps of 64x64 (FP64 oracle restatement, radix-2 FFT, not "
+                      f"FFTW), {el:.1f} s"}
+
+
+def run_reference(args):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return 0
+    steps = args.steps
+    vals = []
+    for i in range(args.warmup + steps):
+        cb = cpu_baseline(target_s=max(2.0, 60.0 / max(1, args.warmup + steps)))
+        if i >= args.warmup:
+            vals.append(cb)
+    v = statistics.median(c["value"] for c in vals)
+    ms = 1e3 * (NTRAJ * NX * NY * FRAME_STEPS) / v
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": CONFIG,
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": vals[0]["cores"], "kind": "port",
+                             "sample": vals[0]["sample"]},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference cannot be built here (FFTW3/Eigen3/cpptoml/CLI11/easylogging++ absent); the "
+                    "arm runs the oracle's FP64 restatement of TWMCBaseSolver's loop on all host threads; "
+                    "ms_per_step extrapolates the per-site rate to one full bench step"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--hop", default="fft", choices=["fft", "stencil"])
+    ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = env_rank()
+    if args.impl == "reference":
+        return run_reference(args)
+    if world > 1:
+        os.environ["CUDA_VISIBLE_DEVICES"] = str(local)
+    import torch
+
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    torch.cuda.set_device(0)
+    from pincosimulator_gb300 import build_ext, twmc
+
+    build_ext.build()
+    fp32_peak = twmc.measure_fp32_peak()
+    sysd = make_system(twmc, twmc.HOP_STENCIL if args.hop == "stencil" else None)
+    tasks = sysd.make_tasks(NTRAJ, t_start=0.0, t_end=T_END, seed0=1000 + rank * NTRAJ, id0=1 + rank * NTRAJ)
+    sysd.batch_init(tasks)
+    for _ in range(max(args.warmup, 3)):
+        sysd.advance(FRAME_STEPS)
+        sysd.reduce()
+    sysd.sync()
+    ext = torch.cuda.ExternalStream(sysd.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    clk_path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "_work",
+                            f"clocks_rank{rank}.csv")
+    os.makedirs(os.path.dirname(clk_path), exist_ok=True)
+    proc, fh = clock_sampler_start(clk_path)
+    time.sleep(0.5)
+    launches0 = sysd.launch_count
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    e0.record(ext)
+    for _ in range(args.steps):
+        sysd.advance(FRAME_STEPS)
+        sysd.reduce()
+    e1.record(ext)
+    kernel_ms = sysd.sync()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    elapsed_ms = e0.elapsed_time(e1)
+    launches = sysd.launch_count - launches0
+    clocks = clock_sampler_stop(proc, fh, clk_path, int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0])
+                                if world > 1 else 0)
+    field, _ = sysd.download(field=True, moments=False)
+    import numpy as np
+
+    finite = bool(np.isfinite(field).all())
+    del field
+    info_kernel = sysd.kernel_name
+    sysd.close()
+    su_rank = float(args.steps) * FRAME_STEPS * NTRAJ * NX * NY
+    t_max = elapsed_ms
+    if dist:
+        t = torch.tensor([elapsed_ms], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_max = float(t.item())
+    value = su_rank * world / (t_max / 1e3)
+    # roofline of the dominant kernel (the step kernel; the moments kernel is < 1%)
+    achieved = su_rank * FLOPS_PER_SITE_UPDATE / (kernel_ms / 1e3) / 1e12
+    # end to end through the C ABI with host buffers (twmc_run)
+    e2e = None
+    if rank == 0 or world > 1:
+        sysd = make_system(twmc, twmc.HOP_STENCIL if args.hop == "stencil" else None)
+        tasks = sysd.make_tasks(NTRAJ, t_start=0.0, t_end=args.e2e_steps * FRAME_STEPS * DT, seed0=7,
+                                store_initial=False)
+        t0 = time.perf_counter()
+        res = sysd.run(tasks, frames=False, final=True, moments=True)
+        el = time.perf_counter() - t0
+        sysd.close()
+        n_fr = args.e2e_steps
+        h2d = (NTRAJ * (8 + 8) + 5 * 2 * NX * NY * 16) / n_fr
+        d2h = (res["final"].size * 8 + n_fr * 32 * NX * NY * 3 * 8 + NTRAJ * (8 + 8 + 4)) / n_fr
+        e2e = {"value": n_fr * FRAME_STEPS * NTRAJ * NX * NY / el, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h), "api": "twmc_run (host buffers: final field complex64->complex128, "
+               "FP64 moment blocks every frame)"}
+        del res
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return 0
+    peaks = measured_peaks()
+    cpu = None if (args.no_cpu_baseline or world > 1) else cpu_baseline()
+    hbm = peaks.get("hbm_gbs")
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox disorder / noise)",
+        "config": dict(CONFIG, hop=args.hop, kernel=info_kernel),
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": achieved / fp32_peak if fp32_peak else None, "traffic": ncu_traffic(),
+                     "peak_source": "measured in this run: FP32 FMA chain over all SMs (twmc_measure_fp32_peak)",
+                     "flops_per_site_update": FLOPS_PER_SITE_UPDATE,
+                     "hbm": {"achieved_gbs": su_rank * BYTES_PER_SITE_UPDATE_HBM / (kernel_ms / 1e3) / 1e9,
+                             "peak_gbs": hbm, "source": "MEASURED_PEAKS.json" if hbm else None}},
+        "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu, "clocks": clocks,
+        "trajectories_per_s": value / (NX * NY * (T_END / DT)), "finite": finite,
+        "kernel_ms": kernel_ms,
+    }
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,209 @@
+/*
+ * twmc.h -- C ABI of libtwmc_cuda.so, the GB300 (sm_103a) Truncated Wigner
+ * Monte Carlo trajectory engine.
+ *
+ * It replaces the per-trajectory hot path of the reference's TWMC solvers
+ * (paths relative to the PincoSimulator project root):
+ *   - TWMCBaseSolver::Compute  src/TWMC/Solvers/TWMCBaseSolver.cpp:94-283
+ *     (1-D chain / 2-D square lattice, FFT hopping, Euler-Maruyama step)
+ *   - TWMCLiebSolver::Compute  src/TWMC/Solvers/TWMCLiebSolver.cpp:109-299
+ *     (1-D Lieb lattice, real-space coupling, optional F(t))
+ * behind the reference's plugin interface Solver::Setup/Compute/
+ * ApproximateComputationProgress (src/Base/Solver.hpp:16-31). A C++ Solver
+ * subclass (pincosimulator_gb300/host) or any FFI caller packs the reference's
+ * TWMCTaskData into twmc_task_desc and calls twmc_run.
+ *
+ * Conventions
+ *   - Complex arrays are interleaved doubles (re, im), i.e. the memory layout
+ *     of std::complex<double> / the reference's complex_p.
+ *   - Site order is the reference's row-major MatrixCXd order: site
+ *     p = i * ny + j on an nx x ny lattice after TWMCSystemData's 1-D swap
+ *     (a chain is nx = 1, ny = N; TWMCSystemData.cpp:25-37); on the Lieb
+ *     lattice p = 3 * cell + {0:A, 1:B, 2:C}.
+ *   - All buffers are owned by the caller. Return codes: 0 = OK, < 0 error.
+ *     No C++ exception crosses this boundary.
+ *   - A handle is not internally synchronised: calls on one handle must be
+ *     serialised by the caller; different handles are independent.
+ */
+#ifndef TWMC_H
+#define TWMC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TWMC_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define TWMC_API __attribute__((visibility("default")))
+#else
+#define TWMC_API
+#endif
+
+enum twmc_status {
+  TWMC_OK = 0,
+  TWMC_ERR_INVALID = -1,     /* bad argument / unsupported combination */
+  TWMC_ERR_CUDA = -2,        /* CUDA runtime error (message in twmc_last_error) */
+  TWMC_ERR_TIMEOUT = -3,     /* a bounded device-side wait gave up */
+  TWMC_ERR_NONFINITE = -4,   /* a trajectory became NaN/Inf (per-task status) */
+  TWMC_ERR_NOMEM = -5,       /* device allocation failed */
+  TWMC_ERR_NOT_BUILT = -6    /* the kernel variant for this shape is not compiled in */
+};
+
+enum twmc_lattice {
+  TWMC_LATTICE_SQUARE = 0, /* 1-D chain or 2-D square lattice (TWMCBaseSolver) */
+  TWMC_LATTICE_LIEB = 1    /* 1-D Lieb lattice, 3 sites per cell (TWMCLiebSolver) */
+};
+
+enum twmc_precision { TWMC_PREC_F32 = 0, TWMC_PREC_F64 = 1 };
+
+enum twmc_noise_mode {
+  TWMC_NOISE_PHILOX = 0, /* in-kernel Philox4x32-10 keyed by (seed, id), counter (site, step, stream) */
+  TWMC_NOISE_BUFFER = 1  /* caller-supplied Wiener increments (deterministic-noise mode) */
+};
+
+enum twmc_hop_mode {
+  TWMC_HOP_FFT = 0,     /* square lattice: on-chip FFT, k-space multiply, inverse FFT (the reference's algorithm) */
+  TWMC_HOP_STENCIL = 1  /* square lattice: the same operator applied in real space (nearest neighbours) */
+};
+
+enum twmc_ic_kind {
+  TWMC_IC_SETTINGS = 0,  /* ReadFromSettings: beta = beta_init + beta_init_sigma * xi (xi from the init stream) */
+  TWMC_IC_FIXED = 1,     /* FixedPoint: beta = beta_init */
+  TWMC_IC_GIVEN = 2      /* ReadFromPreviousData / caller-given field: beta = init_field */
+};
+
+enum twmc_noise_kind { TWMC_DISORDER_NONE = 0, TWMC_DISORDER_GAUSSIAN = 1, TWMC_DISORDER_UNIFORM = 2 };
+
+/* One noisy parameter matrix (NoisyMatrix, src/Base/NoisyMatrix.cpp:118-162):
+ * value = base + noise, noise drawn per trajectory on its own Philox stream. */
+typedef struct twmc_matrix {
+  const double* base;      /* n_sites complex; NULL = all zero */
+  int32_t noise_kind;      /* twmc_noise_kind */
+  const double* noise_amp; /* n_sites complex amplitudes (Re scales the real draw, Im the imaginary) */
+} twmc_matrix;
+
+typedef struct twmc_system_desc {
+  int32_t lattice;     /* twmc_lattice */
+  int64_t nx, ny;      /* lattice (Lieb: cells = nx * ny, sites = 3 * cells) */
+  int32_t pbc;         /* Lieb: periodic boundary (the square lattice is always periodic) */
+  double J;            /* square lattice hopping */
+  double J_AB, J_BC;   /* Lieb couplings */
+  double gamma;        /* loss rate */
+  double detuning;     /* Lieb: delta = detuning - E */
+  double dt;           /* timestep */
+  int64_t frame_steps; /* steps between saved frames (TWMCSystemData::frame_steps) */
+  twmc_matrix omega;   /* square: omega; Lieb: E */
+  twmc_matrix U;
+  twmc_matrix F;
+  twmc_matrix beta_init;
+  twmc_matrix beta_init_sigma;
+  /* Optional F(t) table (NoisyMatrix::SetTemporalValue): ft_nrec records at
+   * ft_times (ascending), ft_values = ft_nrec x n_sites complex; NaN entries
+   * are gap-filled as the reference does. Lieb lattice only. */
+  int64_t ft_nrec;
+  const double* ft_times;
+  const double* ft_values;
+  int32_t precision;   /* twmc_precision */
+  int32_t noise_mode;  /* twmc_noise_mode */
+  int32_t hop_mode;    /* twmc_hop_mode (square lattice) */
+  int32_t n_moment_blocks; /* ensemble blocks for standard errors (0 = 32) */
+} twmc_system_desc;
+
+typedef struct twmc_task_desc {
+  uint64_t id;            /* TWMCTaskData::id (also the second Philox key word, low 32 bits) */
+  uint32_t seed;          /* TWMCTaskData::rngSeed (first Philox key word) */
+  int32_t ic_kind;        /* twmc_ic_kind */
+  double t_start, t_end;  /* TWMCTaskData::t_start / t_end */
+  int32_t store_initial;  /* TWMCTaskData::storeInitialState */
+  const double* init_field; /* TWMC_IC_GIVEN: n_sites complex */
+  const double* U_realization;     /* optional given disorder realisations (n_sites complex), e.g. */
+  const double* omega_realization; /* on continuation (TWMCBaseSolver.cpp:185-199); NULL = draw */
+  const double* F_realization;
+} twmc_task_desc;
+
+typedef struct twmc_outputs {
+  double* frames;          /* optional: n_tasks x n_frames x n_sites complex128 (the "traj" dataset) */
+  double* final_field;     /* optional: n_tasks x n_sites complex */
+  double* U_realization;   /* optional: n_tasks x n_sites complex (U_Realization dataset) */
+  double* omega_realization; /* optional: n_tasks x n_sites complex (Omega_Realization dataset) */
+  double* F_realization;   /* optional: n_tasks x n_sites complex (F_Realizatio dataset) */
+  double* moments;         /* optional: n_frames x n_moment_blocks x n_sites x 3 FP64 sums of
+                              |a|^2, |a|^4 and |a_k|^2 (unitary FFT; 0 on the Lieb lattice) */
+  int64_t* frames_written; /* optional: n_tasks (frames actually produced) */
+  double* t_final;         /* optional: n_tasks (extraDataMemory[1]) */
+  int32_t* status;         /* optional: n_tasks (0 or TWMC_ERR_NONFINITE) */
+} twmc_outputs;
+
+typedef struct twmc_handle twmc_handle;
+
+/* Version of this ABI (TWMC_ABI_VERSION). */
+TWMC_API int twmc_version(void);
+
+/* Builds a solver for one system (TWMCBaseSolver::Setup / TWMCLiebSolver::Setup,
+ * TWMCBaseSolver.cpp:24-92, TWMCLiebSolver.cpp:29-104): uploads the k-space
+ * table or coupling, parameters and F(t) table, selects the kernel. */
+TWMC_API int twmc_create(const twmc_system_desc* desc, twmc_handle** out);
+
+/* Runs n tasks to completion (Solver::Compute, Solver.hpp:22). Tasks are
+ * grouped by (t_start, t_end, store_initial) and each group runs as one
+ * batch on the GPU. Outputs are written in task order. */
+TWMC_API int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs* out);
+
+/* Deterministic-noise mode: Wiener increments for the next twmc_run, laid out
+ * [task][step][site] complex (the reference's randCMat draws,
+ * TWMCBaseSolver.cpp:285-291). count = number of complex values. The buffer is
+ * copied; steps beyond the supplied range are an error. */
+TWMC_API int twmc_set_noise_buffer(twmc_handle* h, const double* xi, size_t count);
+
+/* Fraction of the current/last twmc_run completed (ApproximateComputationProgress). */
+TWMC_API int twmc_progress(const twmc_handle* h, double* fraction);
+
+/* Message of the last error on this handle ("" if none). */
+TWMC_API const char* twmc_last_error(const twmc_handle* h);
+
+TWMC_API void twmc_destroy(twmc_handle* h);
+
+/* ---- device-resident batch API (inputs and state stay in HBM) ---------- */
+
+/* Allocates and initialises a device batch of n trajectories for the tasks
+ * (initial fields and disorder drawn on the GPU). */
+TWMC_API int twmc_batch_init(twmc_handle* h, const twmc_task_desc* tasks, size_t n);
+/* Advances the batch by n_steps steps (asynchronous on the handle's stream). */
+TWMC_API int twmc_batch_advance(twmc_handle* h, int64_t n_steps);
+/* Reduces the current batch state into FP64 moment blocks (asynchronous). */
+TWMC_API int twmc_batch_reduce(twmc_handle* h);
+/* Waits for the handle's stream; *kernel_ms = summed device time of the
+ * trajectory-step launches since the last call (may be NULL). */
+TWMC_API int twmc_sync(twmc_handle* h, double* kernel_ms);
+/* Copies the batch state (n x n_sites complex128) and/or the last moment
+ * blocks (n_moment_blocks x n_sites x 3) to host memory; NULL skips. */
+TWMC_API int twmc_batch_download(twmc_handle* h, double* field, double* moments);
+/* Kernel launches issued by this handle since creation (trajectory steps,
+ * reductions, initialisation). */
+TWMC_API int64_t twmc_launch_count(const twmc_handle* h);
+/* Name of the step kernel variant the handle selected. */
+TWMC_API const char* twmc_kernel_name(const twmc_handle* h);
+/* The CUDA stream (cudaStream_t) all of the handle's work is issued on, for
+ * callers that order their own work or record events against it. */
+TWMC_API void* twmc_stream(const twmc_handle* h);
+
+/* FP32 FMA throughput of the current device in TFLOP/s, measured with a
+ * register-resident FMA chain over all SMs (the CUDA-core roofline of the
+ * step kernels). */
+TWMC_API int twmc_measure_fp32_peak(double* tflops);
+
+/* ---- self-check entry points -------------------------------------------- */
+
+/* Philox4x32-10 evaluated on the GPU for n counters (ctr: n x 4, key: 2 words),
+ * out: n x 4 words. */
+TWMC_API int twmc_debug_philox(const uint32_t* ctr, size_t n, const uint32_t* key, uint32_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TWMC_H */

@@ -1,0 +1,94 @@
+// twmc_common.cuh -- shared device helpers of the TWMC engine: complex
+// arithmetic in FP32/FP64, Philox4x32-10 and the Box-Muller normal pairs.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <type_traits>
+#include <utility>
+
+namespace twmc {
+
+template <typename R> struct C2;
+template <> struct C2<float> { using type = float2; };
+template <> struct C2<double> { using type = double2; };
+template <typename R> using c2_t = typename C2<R>::type;
+
+template <typename T> __device__ __forceinline__ T cmake(decltype(T::x) x, decltype(T::x) y) { T r; r.x = x; r.y = y; return r; }
+template <typename T> __device__ __forceinline__ T cadd(T a, T b) { return cmake<T>(a.x + b.x, a.y + b.y); }
+template <typename T> __device__ __forceinline__ T csub(T a, T b) { return cmake<T>(a.x - b.x, a.y - b.y); }
+template <typename T> __device__ __forceinline__ T cmul(T a, T b) { return cmake<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
+// a * conj(b)
+template <typename T> __device__ __forceinline__ T cmulc(T a, T b) { return cmake<T>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }
+// -i * a and +i * a
+template <typename T> __device__ __forceinline__ T cmul_mi(T a) { return cmake<T>(a.y, -a.x); }
+template <typename T> __device__ __forceinline__ T cmul_pi(T a) { return cmake<T>(-a.y, a.x); }
+
+// Compile-time loop: f(std::integral_constant<int, I>) for I = 0..N-1.
+template <class F, int... Is>
+__device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, Is...>) {
+  (f(std::integral_constant<int, Is>{}), ...);
+}
+template <int N, class F>
+__device__ __forceinline__ void static_for(F&& f) {
+  static_for_impl(f, std::make_integer_sequence<int, N>{});
+}
+
+// ---------------------------------------------------------------------------
+// Philox4x32-10 (Salmon et al., SC'11): 10 rounds of two 32x32->64-bit
+// multiplies with Weyl-sequence key bumps. Counter (c0,c1,c2,c3), key (k0,k1).
+// ---------------------------------------------------------------------------
+struct u32x4 { uint32_t x, y, z, w; };
+
+__host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint32_t k0, uint32_t k1) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+    const uint32_t lo0 = 0xD2511F53u * c.x, hi0 = __umulhi(0xD2511F53u, c.x);
+    const uint32_t lo1 = 0xCD9E8D57u * c.z, hi1 = __umulhi(0xCD9E8D57u, c.z);
+#else
+    const uint64_t p0 = uint64_t(0xD2511F53u) * c.x, p1 = uint64_t(0xCD9E8D57u) * c.z;
+    const uint32_t lo0 = uint32_t(p0), hi0 = uint32_t(p0 >> 32);
+    const uint32_t lo1 = uint32_t(p1), hi1 = uint32_t(p1 >> 32);
+#endif
+    c = u32x4{hi1 ^ c.y ^ k0, lo1, hi0 ^ c.w ^ k1, lo0};
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  return c;
+}
+
+// Noise streams (counter word 2).
+enum : uint32_t { kStreamWiener = 0, kStreamInit = 1, kStreamU = 2, kStreamOmega = 3, kStreamF = 4 };
+
+// Box-Muller, FP32: u = fma(float(w), 2^-32, 2^-33) in (0, 1]; angle in [-pi, pi).
+__device__ __forceinline__ float2 normal_pair(uint32_t a, uint32_t b, float) {
+  const float u1 = __fmaf_rn(__uint2float_rn(a), 0x1p-32f, 0x1p-33f);
+  const float u2 = __fmaf_rn(__uint2float_rn(b), 0x1p-32f, 0x1p-33f);
+  const float th = __fmaf_rn(u2, 6.28318530717958647692f, -3.14159265358979323846f);
+  const float r = sqrtf(fmaxf(-2.0f * logf(u1), 0.0f));
+  float s, c;
+  __sincosf(th, &s, &c);
+  return make_float2(r * c, r * s);
+}
+
+// Box-Muller, FP64: u = (w + 1/2) 2^-32.
+__device__ __forceinline__ double2 normal_pair(uint32_t a, uint32_t b, double) {
+  const double u1 = (double(a) + 0.5) * 0x1p-32;
+  const double u2 = (double(b) + 0.5) * 0x1p-32;
+  const double r = sqrt(-2.0 * log(u1));
+  const double th = 6.283185307179586476925 * u2 - 3.141592653589793238463;
+  double s, c;
+  sincos(th, &s, &c);
+  return make_double2(r * c, r * s);
+}
+
+// Site pairing on Philox calls: half = ceil(n/2); site p < half uses words
+// (0,1) of call p, site p >= half words (2,3) of call p - half.
+__host__ __device__ __forceinline__ uint32_t site_ctr(int64_t p, int64_t n, int* hi) {
+  const int64_t half = (n + 1) / 2;
+  *hi = p >= half;
+  return uint32_t(p >= half ? p - half : p);
+}
+
+}  // namespace twmc

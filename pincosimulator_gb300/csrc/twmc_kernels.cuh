@@ -1,0 +1,585 @@
+// twmc_kernels.cuh -- trajectory step kernels of the TWMC engine.
+//
+// square_fft_kernel: the per-trajectory Euler-Maruyama step of the
+//   reference's TWMCBaseSolver (TWMCBaseSolver.cpp:232-266):
+//     X = FFT(beta); X *= -i 2J (cos kx + cos ky); h = IFFT(X)/N;
+//     a = ((-i omega - gamma/2 + i U (|beta|^2 - 1)) beta + h + i F) dt;
+//     beta += a + sqrt(gamma dt / 4) xi
+//   Each trajectory's lattice stays in registers for the whole launch
+//   (hundreds of steps); the FFT runs as register-resident radix-4/2 DIF
+//   passes with shared-memory exchanges between passes (plans from
+//   fft_plan.py). HBM is touched only at the start and end of a launch.
+// ell_kernel: the same step with the hopping applied in real space from a
+//   neighbour list: the reference's Lieb solver (TWMCLiebSolver.cpp:250-280,
+//   h = -i (beta C)) including the time-tabulated F(t), and the square
+//   lattice for any nx, ny (the FFT operator above is exactly the
+//   nearest-neighbour stencil -i J sum_nn beta).
+#pragma once
+
+#include "twmc_common.cuh"
+
+namespace twmc {
+
+// ------------------------------------------------------------------------
+// arguments
+// ------------------------------------------------------------------------
+struct StepArgs {
+  void* state;            // [ntraj][N] complex (R)
+  int64_t ntraj;
+  int64_t nsteps;         // steps in this launch
+  uint32_t step0;         // global index of the first step (Philox counter word 1)
+  const uint32_t* seeds;  // [ntraj] Philox key word 0
+  const uint32_t* ids;    // [ntraj] Philox key word 1
+  // per-site parameters (complex R); NULL = use the scalar value
+  const void* rsl;        // -i omega - gamma/2   (Lieb: -i (detuning - E) - gamma/2)
+  const void* iU;         // i U
+  const void* iF;         // i F
+  int64_t par_stride;     // elements between trajectories (0 = shared)
+  double rsl_s[2], iU_s[2], iF_s[2];
+  double dt, dt4;
+  // noise
+  int noise_mode;         // 0 Philox, 1 buffer
+  const void* noise;      // [ntraj][noise_steps][N] complex (R)
+  int64_t noise_traj_stride;  // = noise_steps * N
+  // outputs
+  void* nk;               // optional [ntraj][N] R: |FFT(beta)|^2 / N of the final state
+  int* status;            // [ntraj]
+  // square FFT kernel tables
+  const void* tw;         // [M0 + M1] complex R: W_M^j per dimension
+  const void* ktab;       // [E][TPT] R: 2J(cos kx + cos ky)/N at last-pass positions
+  // ell kernel
+  int tpt;                // threads per trajectory
+  int64_t nsites;         // N
+  int64_t nx, ny;         // square-stencil geometry
+  int hop_kind;           // 0 = neighbour table, 1 = square stencil
+  const int* nbr_idx;     // [N][4]
+  const void* nbr_w;      // [N][4] complex R (h = sum w beta_idx)
+  double J;
+  // F(t) (ell kernel)
+  const void* ft_vals;    // [(nrec+1)][N] complex R: i F at the records
+  const void* ft_slopes;  // [(nrec+1)][N] complex R: i dF/dt
+  const int* ft_id;       // [total steps] segment id per step
+  const double* ft_dt;    // [total steps] t - t_id per step
+  int dbuf;               // ell: double-buffered exchange
+};
+
+__device__ __forceinline__ void set_status(int* status, int64_t traj, bool bad) {
+  if (bad && status) status[traj] = -4;  // TWMC_ERR_NONFINITE
+}
+
+template <typename T>
+__device__ __forceinline__ bool finite_c(T v) {
+  return isfinite(v.x) && isfinite(v.y);
+}
+
+// Local Euler-Maruyama update, the reference's operation order
+// (TWMCBaseSolver.cpp:245-253): a = ((rsl + iU (|b|^2-1)) b + h + iF) dt;
+// b = b + a + dt4 xi.
+template <typename T, typename R>
+__device__ __forceinline__ T local_update(T b, T h, T rsl, T iU, T iF, R dt, R dt4, T xi) {
+  const R ab2 = b.x * b.x + b.y * b.y;
+  const R f = ab2 - R(1);
+  const T c = cmake<T>(rsl.x + iU.x * f, rsl.y + iU.y * f);
+  T s = cmul(c, b);
+  s = cadd(s, h);
+  s = cadd(s, iF);
+  const T a = cmake<T>(s.x * dt, s.y * dt);
+  T nb = cadd(b, a);
+  return cmake<T>(nb.x + dt4 * xi.x, nb.y + dt4 * xi.y);
+}
+
+// ------------------------------------------------------------------------
+// compile-time plan helpers (P = generated Plan_bx_by)
+// ------------------------------------------------------------------------
+template <class P> struct PlanInfo {
+  static constexpr int E = 1 << P::e;
+  static constexpr int N = 1 << P::nbits;
+  static constexpr int TPT = N / E;
+  static constexpr int M0 = 1 << P::m[0];
+  static constexpr int M1 = 1 << P::m[1];
+  static constexpr int slot_bit(int k, int g) {
+    for (int j = 0; j < P::e; ++j) if (P::reg[k][j] == g) return j;
+    return -1;
+  }
+  static constexpr int pos_reg(int k, int s) {
+    int p = 0;
+    for (int j = 0; j < P::e; ++j) p |= ((s >> j) & 1) << P::reg[k][j];
+    return p;
+  }
+  static constexpr uint32_t thr_mask(int k) {
+    uint32_t m = 0;
+    for (int i = 0; i < P::nthr; ++i) m |= 1u << P::thr[k][i];
+    return P::nthr ? m : 0u;
+  }
+  // slot index with zero bits inserted at positions j0 (and j1 if >= 0)
+  static constexpr int insert0(int q, int j0, int j1) {
+    int s = 0, src = 0;
+    for (int j = 0; j < P::e; ++j) {
+      if (j == j0 || j == j1) continue;
+      s |= ((q >> src) & 1) << j;
+      ++src;
+    }
+    return s;
+  }
+};
+
+// Swizzle of the CTA-flat element index (XOR of bits 4..7 into 0..3): linear
+// over XOR, so thread and register parts are swizzled separately.
+template <int FLAT_BITS>
+__host__ __device__ constexpr int swz(int p) {
+  return FLAT_BITS >= 8 ? (p ^ ((p >> 4) & 15)) : p;
+}
+
+// One DIF stage (forward) or its adjoint (inverse) of pass K, stage SI.
+template <class P, int K, int SI, bool INV, typename T>
+__device__ __forceinline__ void fft_stage(T (&x)[PlanInfo<P>::E], const T* __restrict__ tw0,
+                                          const T* __restrict__ tw1, int pos_thr) {
+  using I = PlanInfo<P>;
+  constexpr int dim = P::st[K][SI][0];
+  constexpr int t = P::st[K][SI][1];
+  constexpr int rb = P::st[K][SI][2];
+  constexpr int lo = P::lo[dim];
+  constexpr int m = P::m[dim];
+  constexpr uint32_t lowmask = ((1u << t) - 1u) << lo;  // global bits of local bits < t
+  constexpr bool thr_low = (I::thr_mask(K) & lowmask) != 0u;
+  const T* __restrict__ tw = dim ? tw1 : tw0;
+  const int low_t = thr_low ? int((uint32_t(pos_thr) & lowmask) >> lo) : 0;
+  if constexpr (rb == 2) {
+    constexpr int j0 = I::slot_bit(K, lo + t);
+    constexpr int j1 = I::slot_bit(K, lo + t + 1);
+    static_assert(j0 >= 0 && j1 >= 0, "stage bits must be register bits");
+    constexpr int sh = m - t - 2;
+    static_for<I::E / 4>([&](auto Q) {
+      constexpr int s0 = I::insert0(decltype(Q)::value, j0, j1);
+      constexpr int s1 = s0 | (1 << j0), s2 = s0 | (1 << j1), s3 = s0 | (1 << j0) | (1 << j1);
+      constexpr int low_r = int((uint32_t(I::pos_reg(K, s0)) & lowmask) >> lo);
+      constexpr bool trivial = !thr_low && low_r == 0;
+      T w1, w2, w3;
+      if constexpr (!trivial) {
+        const int e1 = (low_r + low_t) << sh;
+        w1 = tw[e1];
+        w2 = tw[2 * e1];
+        w3 = tw[3 * e1];
+      }
+      if constexpr (!INV) {
+        const T A = cadd(x[s0], x[s2]), B = cadd(x[s1], x[s3]);
+        const T C = csub(x[s0], x[s2]), D = csub(x[s1], x[s3]);
+        T y0 = cadd(A, B), y1 = csub(A, B);
+        T y2 = cmake<T>(C.x + D.y, C.y - D.x);  // C - iD
+        T y3 = cmake<T>(C.x - D.y, C.y + D.x);  // C + iD
+        if constexpr (!trivial) {
+          y1 = cmul(y1, w2);
+          y2 = cmul(y2, w1);
+          y3 = cmul(y3, w3);
+        }
+        x[s0] = y0; x[s1] = y1; x[s2] = y2; x[s3] = y3;
+      } else {
+        T u = x[s1], p = x[s2], q = x[s3];
+        if constexpr (!trivial) {
+          u = cmulc(u, w2);
+          p = cmulc(p, w1);
+          q = cmulc(q, w3);
+        }
+        const T A = cadd(x[s0], u), B = csub(x[s0], u);
+        const T C = cadd(p, q);
+        const T pq = csub(p, q);
+        const T D = cmake<T>(-pq.y, pq.x);  // i (p - q)
+        x[s0] = cadd(A, C); x[s2] = csub(A, C); x[s1] = cadd(B, D); x[s3] = csub(B, D);
+      }
+    });
+  } else {
+    constexpr int j0 = I::slot_bit(K, lo + t);
+    static_assert(j0 >= 0, "stage bit must be a register bit");
+    constexpr int sh = m - t - 1;
+    static_for<I::E / 2>([&](auto Q) {
+      constexpr int s0 = I::insert0(decltype(Q)::value, j0, -1);
+      constexpr int s1 = s0 | (1 << j0);
+      constexpr int low_r = int((uint32_t(I::pos_reg(K, s0)) & lowmask) >> lo);
+      constexpr bool trivial = !thr_low && low_r == 0;
+      T w;
+      if constexpr (!trivial) w = tw[(low_r + low_t) << sh];
+      if constexpr (!INV) {
+        T y0 = cadd(x[s0], x[s1]), y1 = csub(x[s0], x[s1]);
+        if constexpr (!trivial) y1 = cmul(y1, w);
+        x[s0] = y0; x[s1] = y1;
+      } else {
+        T u = x[s1];
+        if constexpr (!trivial) u = cmulc(u, w);
+        const T y0 = x[s0];
+        x[s0] = cadd(y0, u); x[s1] = csub(y0, u);
+      }
+    });
+  }
+}
+
+template <class P, int K, bool INV, typename T>
+__device__ __forceinline__ void fft_pass(T (&x)[PlanInfo<P>::E], const T* tw0, const T* tw1, int pos_thr) {
+  constexpr int ns = P::nst[K];
+  static_for<ns>([&](auto S) {
+    constexpr int si = INV ? (ns - 1 - decltype(S)::value) : decltype(S)::value;
+    fft_stage<P, K, si, INV>(x, tw0, tw1, pos_thr);
+  });
+}
+
+// Exchange from layout of pass KA to layout of pass KB through shared memory.
+template <class P, int KA, int KB, int FLAT_BITS, bool SYNC_WARP, typename T>
+__device__ __forceinline__ void fft_exchange(T (&x)[PlanInfo<P>::E], T* __restrict__ buf, int base_a,
+                                             int base_b) {
+  using I = PlanInfo<P>;
+  static_for<I::E>([&](auto S) {
+    constexpr int s = decltype(S)::value;
+    constexpr int off = swz<FLAT_BITS>(I::pos_reg(KA, s));
+    buf[base_a ^ off] = x[s];
+  });
+  if constexpr (SYNC_WARP) __syncwarp(); else __syncthreads();
+  static_for<I::E>([&](auto S) {
+    constexpr int s = decltype(S)::value;
+    constexpr int off = swz<FLAT_BITS>(I::pos_reg(KB, s));
+    x[s] = buf[base_b ^ off];
+  });
+}
+
+template <class P, int CTA>
+struct SquareCfg {
+  using I = PlanInfo<P>;
+  static constexpr int E = I::E, N = I::N, TPT = I::TPT;
+  static constexpr int TPC = CTA / TPT;  // trajectories per CTA
+  static constexpr int FLAT_BITS = P::nbits + (TPC > 1 ? (TPC == 2 ? 1 : TPC == 4 ? 2 : TPC == 8 ? 3 : TPC == 16 ? 4 : TPC == 32 ? 5 : TPC == 64 ? 6 : 7) : 0);
+  static constexpr bool SYNC_WARP = TPT <= 32;
+  template <typename R>
+  static constexpr size_t smem_bytes(int nparams) {
+    using T = c2_t<R>;
+    return sizeof(T) * (size_t(I::M0 + I::M1) + 2 * size_t(TPC) * N + size_t(nparams) * TPC * N) +
+           sizeof(R) * size_t(N);
+  }
+};
+
+template <typename R, class P, int CTA>
+__global__ void __launch_bounds__(CTA) square_fft_kernel(const StepArgs a) {
+  using T = c2_t<R>;
+  using I = PlanInfo<P>;
+  using Cfg = SquareCfg<P, CTA>;
+  constexpr int E = I::E, N = I::N, TPT = I::TPT, TPC = Cfg::TPC;
+  constexpr int NP = P::npass;
+  constexpr int LAST = NP - 1;
+  static_assert(CTA % TPT == 0, "CTA must hold whole trajectories");
+  static_assert(P::reg[0][P::e - 1] == P::nbits - 1, "top bit must be a register bit of the first pass");
+
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s_tw = reinterpret_cast<T*>(smem_raw);
+  T* s_x = s_tw + (I::M0 + I::M1);         // 2 exchange buffers of TPC * N
+  T* s_par = s_x + 2 * TPC * N;             // per-site params, thread-private slices
+  const bool has_rsl = a.rsl != nullptr, has_iU = a.iU != nullptr, has_iF = a.iF != nullptr;
+  // per-site parameters live in thread-private smem slices when they fit
+  // (a.dbuf = 1), else they are read from global memory every step
+  const bool par_smem = a.dbuf != 0;
+  const int nparams = par_smem ? int(has_rsl) + int(has_iU) + int(has_iF) : 0;
+  R* s_k = reinterpret_cast<R*>(s_par + nparams * TPC * N);
+
+  const int tid = threadIdx.x;
+  const int slot = tid / TPT;
+  const int t = tid % TPT;
+
+  // tables
+  for (int i = tid; i < I::M0 + I::M1; i += CTA) s_tw[i] = reinterpret_cast<const T*>(a.tw)[i];
+  for (int i = tid; i < N; i += CTA) s_k[i] = reinterpret_cast<const R*>(a.ktab)[i];
+  __syncthreads();
+  const T* tw0 = s_tw;
+  const T* tw1 = s_tw + I::M0;
+
+  // thread part of each pass's positions, and exchange bases
+  int pos_thr[NP];
+  int xbase[NP];
+  static_for<NP>([&](auto KK) {
+    constexpr int k = decltype(KK)::value;
+    int p = 0;
+    static_for<P::nthr>([&](auto II) {
+      constexpr int i = decltype(II)::value;
+      constexpr int b = P::thr[k][i];
+      p |= ((t >> i) & 1) << b;
+    });
+    pos_thr[k] = p;
+    xbase[k] = swz<Cfg::FLAT_BITS>((slot << P::nbits) | p);
+  });
+
+  const R dt = R(a.dt), dt4 = R(a.dt4);
+  const T rsl_s = cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
+  const T iU_s = cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
+  const T iF_s = cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
+  T* par_rsl = s_par;
+  T* par_iU = par_rsl + (has_rsl ? TPC * N : 0);
+  T* par_iF = par_iU + (has_iU ? TPC * N : 0);
+
+  int buf = 0;
+  const int64_t ngroups = (a.ntraj + TPC - 1) / TPC;
+  for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const int64_t traj = g * TPC + slot;
+    const bool active = traj < a.ntraj;
+    const int64_t tr = active ? traj : 0;
+    T* st = reinterpret_cast<T*>(a.state) + tr * N;
+    T beta[E];
+    static_for<E>([&](auto S) {
+      constexpr int s = decltype(S)::value;
+      beta[s] = st[pos_thr[0] | I::pos_reg(0, s)];
+    });
+    // per-site parameters of this trajectory -> thread-private smem slices
+    const T* g_rsl = has_rsl ? reinterpret_cast<const T*>(a.rsl) + tr * a.par_stride : nullptr;
+    const T* g_iU = has_iU ? reinterpret_cast<const T*>(a.iU) + tr * a.par_stride : nullptr;
+    const T* g_iF = has_iF ? reinterpret_cast<const T*>(a.iF) + tr * a.par_stride : nullptr;
+    if (par_smem) {
+      static_for<E>([&](auto S) {
+        constexpr int s = decltype(S)::value;
+        const int p = pos_thr[0] | I::pos_reg(0, s);
+        const int q = (slot * E + s) * TPT + t;
+        if (has_rsl) par_rsl[q] = g_rsl[p];
+        if (has_iU) par_iU[q] = g_iU[p];
+        if (has_iF) par_iF[q] = g_iF[p];
+      });
+    }
+    const uint32_t seed = a.seeds[tr], id = a.ids[tr];
+    const T* noise_tr = reinterpret_cast<const T*>(a.noise) + tr * a.noise_traj_stride;
+
+    for (int64_t step = 0; step < a.nsteps; ++step) {
+      T x[E];
+#pragma unroll
+      for (int s = 0; s < E; ++s) x[s] = beta[s];
+      // forward FFT
+      static_for<NP>([&](auto KK) {
+        constexpr int k = decltype(KK)::value;
+        if constexpr (k > 0) {
+          fft_exchange<P, k - 1, k, Cfg::FLAT_BITS, Cfg::SYNC_WARP>(x, s_x + buf * TPC * N, xbase[k - 1], xbase[k]);
+          buf ^= 1;
+        }
+        fft_pass<P, k, false>(x, tw0, tw1, pos_thr[k]);
+      });
+      // k-space multiply by -i 2J (cos kx + cos ky) / N
+      static_for<E>([&](auto S) {
+        constexpr int s = decltype(S)::value;
+        const R sk = s_k[s * TPT + t];
+        x[s] = cmake<T>(sk * x[s].y, -sk * x[s].x);
+      });
+      // inverse FFT (adjoint passes in reverse order)
+      static_for<NP>([&](auto KK) {
+        constexpr int k = LAST - decltype(KK)::value;
+        fft_pass<P, k, true>(x, tw0, tw1, pos_thr[k]);
+        if constexpr (k > 0) {
+          fft_exchange<P, k, k - 1, Cfg::FLAT_BITS, Cfg::SYNC_WARP>(x, s_x + buf * TPC * N, xbase[k], xbase[k - 1]);
+          buf ^= 1;
+        }
+      });
+      // noise + local update (pass-0 layout: slot bit e-1 is the top site bit)
+      const uint32_t gstep = a.step0 + uint32_t(step);
+      static_for<E / 2>([&](auto Q) {
+        constexpr int s_lo = decltype(Q)::value;          // top slot bit clear
+        constexpr int s_hi = s_lo | (E / 2);
+        T xi_lo, xi_hi;
+        if (a.noise_mode == 0) {
+          const int p = pos_thr[0] | I::pos_reg(0, s_lo);  // p < N/2
+          const u32x4 w = philox4x32_10(u32x4{uint32_t(p), gstep, kStreamWiener, 0u}, seed, id);
+          xi_lo = normal_pair(w.x, w.y, R(0));
+          xi_hi = normal_pair(w.z, w.w, R(0));
+        } else {
+          const T* nz = noise_tr + (int64_t(gstep)) * N;
+          xi_lo = nz[pos_thr[0] | I::pos_reg(0, s_lo)];
+          xi_hi = nz[pos_thr[0] | I::pos_reg(0, s_hi)];
+        }
+        T r_lo = rsl_s, r_hi = rsl_s, u_lo = iU_s, u_hi = iU_s, f_lo = iF_s, f_hi = iF_s;
+        if (par_smem) {
+          const int qlo = (slot * E + s_lo) * TPT + t;
+          const int qhi = (slot * E + s_hi) * TPT + t;
+          if (has_rsl) { r_lo = par_rsl[qlo]; r_hi = par_rsl[qhi]; }
+          if (has_iU) { u_lo = par_iU[qlo]; u_hi = par_iU[qhi]; }
+          if (has_iF) { f_lo = par_iF[qlo]; f_hi = par_iF[qhi]; }
+        } else {
+          const int plo = pos_thr[0] | I::pos_reg(0, s_lo);
+          const int phi = pos_thr[0] | I::pos_reg(0, s_hi);
+          if (has_rsl) { r_lo = __ldg(g_rsl + plo); r_hi = __ldg(g_rsl + phi); }
+          if (has_iU) { u_lo = __ldg(g_iU + plo); u_hi = __ldg(g_iU + phi); }
+          if (has_iF) { f_lo = __ldg(g_iF + plo); f_hi = __ldg(g_iF + phi); }
+        }
+        beta[s_lo] = local_update(beta[s_lo], x[s_lo], r_lo, u_lo, f_lo, dt, dt4, xi_lo);
+        beta[s_hi] = local_update(beta[s_hi], x[s_hi], r_hi, u_hi, f_hi, dt, dt4, xi_hi);
+      });
+    }
+
+    // write back, status
+    bool bad = false;
+    if (active) {
+      static_for<E>([&](auto S) {
+        constexpr int s = decltype(S)::value;
+        st[pos_thr[0] | I::pos_reg(0, s)] = beta[s];
+        bad |= !finite_c(beta[s]);
+      });
+      set_status(a.status, traj, bad);
+    }
+    // |FFT(beta)|^2 / N of the final state for the k-space populations
+    if (a.nk != nullptr) {
+      T x[E];
+#pragma unroll
+      for (int s = 0; s < E; ++s) x[s] = beta[s];
+      static_for<NP>([&](auto KK) {
+        constexpr int k = decltype(KK)::value;
+        if constexpr (k > 0) {
+          fft_exchange<P, k - 1, k, Cfg::FLAT_BITS, Cfg::SYNC_WARP>(x, s_x + buf * TPC * N, xbase[k - 1], xbase[k]);
+          buf ^= 1;
+        }
+        fft_pass<P, k, false>(x, tw0, tw1, pos_thr[k]);
+      });
+      if (active) {
+        R* nk = reinterpret_cast<R*>(a.nk) + traj * N;
+        static_for<E>([&](auto S) {
+          constexpr int s = decltype(S)::value;
+          const uint32_t p = uint32_t(pos_thr[LAST] | I::pos_reg(LAST, s));
+          const uint32_t pc = p & ((1u << P::by) - 1u), pr = p >> P::by;
+          const uint32_t ky = P::by ? (__brev(pc) >> (32 - P::by)) : 0u;
+          const uint32_t kx = P::bx ? (__brev(pr) >> (32 - P::bx)) : 0u;
+          nk[(kx << P::by) | ky] = (x[s].x * x[s].x + x[s].y * x[s].y) / R(N);
+        });
+      }
+    }
+  }
+}
+
+// ------------------------------------------------------------------------
+// real-space hopping kernel (Lieb lattice, square stencil, any N)
+// Thread t of a trajectory holds VPT sites: for v < VPT/2 site t + v*TPT,
+// for v >= VPT/2 site half + t + (v - VPT/2)*TPT (half = ceil(N/2)), so the
+// two sites of one Philox call live in the same thread. Neighbour indices
+// are kept in registers as packed 16-bit pairs (N <= 16384).
+// HOP = 0: neighbour table with complex weights (h = sum_j w_j beta_j);
+// HOP = 1: square stencil h = -i J (wy (b[c+1] + b[c-1]) + wx (b[r+1] + b[r-1])).
+// ------------------------------------------------------------------------
+template <typename R, int VPT, int CTA, int HOP>
+__global__ void __launch_bounds__(CTA) ell_kernel(const StepArgs a) {
+  using T = c2_t<R>;
+  constexpr int H = VPT / 2;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T* s_b = reinterpret_cast<T*>(smem_raw);
+  const int64_t N = a.nsites;
+  const int64_t half = (N + 1) / 2;
+  const int tpt = a.tpt;
+  const int tpc = CTA / tpt;
+  const int tid = threadIdx.x;
+  const int slot = tid / tpt;
+  const int t = tid % tpt;
+  const bool in_slot = slot < tpc;
+
+  int site[VPT];
+  bool valid[VPT];
+#pragma unroll
+  for (int v = 0; v < VPT; ++v) {
+    const int64_t s = v < H ? int64_t(t) + int64_t(v) * tpt : half + int64_t(t) + int64_t(v - H) * tpt;
+    valid[v] = in_slot && (v < H ? s < half : s < N);
+    site[v] = valid[v] ? int(s) : 0;
+  }
+  uint32_t nb01[VPT], nb23[VPT];
+  T nw[HOP == 0 ? VPT : 1][4];
+#pragma unroll
+  for (int v = 0; v < VPT; ++v) {
+    const int p = site[v];
+    int n4[4];
+    if constexpr (HOP == 0) {
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        n4[j] = a.nbr_idx[int64_t(p) * 4 + j];
+        nw[v][j] = reinterpret_cast<const T*>(a.nbr_w)[int64_t(p) * 4 + j];
+      }
+    } else {
+      const int64_t nx = a.nx, ny = a.ny;
+      const int64_t r = p / ny, c = p % ny;
+      n4[0] = int(r * ny + (c + 1) % ny);
+      n4[1] = int(r * ny + (c + ny - 1) % ny);
+      n4[2] = int(((r + 1) % nx) * ny + c);
+      n4[3] = int(((r + nx - 1) % nx) * ny + c);
+    }
+    nb01[v] = uint32_t(n4[0]) | (uint32_t(n4[1]) << 16);
+    nb23[v] = uint32_t(n4[2]) | (uint32_t(n4[3]) << 16);
+  }
+  const R wy = a.ny > 1 ? R(1) : R(0), wx = a.nx > 1 ? R(1) : R(0);
+  const R J = R(a.J);
+  const R dt = R(a.dt), dt4 = R(a.dt4);
+  const T rsl_s = cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
+  const T iU_s = cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
+  const T iF_s = cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
+  const bool timedep = a.ft_vals != nullptr;
+
+  const int64_t ngroups = (a.ntraj + tpc - 1) / tpc;
+  const int64_t slice = N;
+  int buf = 0;
+  for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const int64_t traj = g * tpc + slot;
+    const bool active = in_slot && traj < a.ntraj;
+    const int64_t tr = active ? traj : 0;
+    T* st = reinterpret_cast<T*>(a.state) + tr * N;
+    T beta[VPT], rsl[VPT], iU[VPT], iF[VPT];
+#pragma unroll
+    for (int v = 0; v < VPT; ++v) {
+      const int p = site[v];
+      beta[v] = active && valid[v] ? st[p] : cmake<T>(R(0), R(0));
+      rsl[v] = a.rsl ? reinterpret_cast<const T*>(a.rsl)[tr * a.par_stride + p] : rsl_s;
+      iU[v] = a.iU ? reinterpret_cast<const T*>(a.iU)[tr * a.par_stride + p] : iU_s;
+      iF[v] = a.iF ? reinterpret_cast<const T*>(a.iF)[tr * a.par_stride + p] : iF_s;
+    }
+    const uint32_t seed = a.seeds[tr], id = a.ids[tr];
+    const T* noise_tr = reinterpret_cast<const T*>(a.noise) + tr * a.noise_traj_stride;
+    for (int64_t step = 0; step < a.nsteps; ++step) {
+      const uint32_t gstep = a.step0 + uint32_t(step);
+      T* sb = s_b + (a.dbuf ? buf : 0) * int64_t(tpc) * slice + int64_t(in_slot ? slot : 0) * slice;
+#pragma unroll
+      for (int v = 0; v < VPT; ++v) if (valid[v]) sb[site[v]] = beta[v];
+      __syncthreads();
+      T h[VPT];
+#pragma unroll
+      for (int v = 0; v < VPT; ++v) {
+        const T b0 = sb[nb01[v] & 0xFFFFu], b1 = sb[nb01[v] >> 16];
+        const T b2 = sb[nb23[v] & 0xFFFFu], b3 = sb[nb23[v] >> 16];
+        if constexpr (HOP == 0) {
+          T acc = cmul(nw[v][0], b0);
+          acc = cadd(acc, cmul(nw[v][1], b1));
+          acc = cadd(acc, cmul(nw[v][2], b2));
+          acc = cadd(acc, cmul(nw[v][3], b3));
+          h[v] = acc;
+        } else {
+          const T sy = cadd(b0, b1), sx = cadd(b2, b3);
+          const T s = cmake<T>(wy * sy.x + wx * sx.x, wy * sy.y + wx * sx.y);
+          h[v] = cmake<T>(J * s.y, -J * s.x);  // -i J s
+        }
+      }
+      if (a.dbuf) buf ^= 1; else __syncthreads();
+      if (timedep) {
+        const int id_t = a.ft_id[gstep];
+        const R dtt = R(a.ft_dt[gstep]);
+        const T* fv = reinterpret_cast<const T*>(a.ft_vals) + int64_t(id_t) * N;
+        const T* fs = reinterpret_cast<const T*>(a.ft_slopes) + int64_t(id_t) * N;
+#pragma unroll
+        for (int v = 0; v < VPT; ++v) {
+          const T f0 = fv[site[v]], f1 = fs[site[v]];
+          iF[v] = cmake<T>(f0.x + dtt * f1.x, f0.y + dtt * f1.y);
+        }
+      }
+#pragma unroll
+      for (int v = 0; v < H; ++v) {
+        T xi_lo, xi_hi;
+        if (a.noise_mode == 0) {
+          const u32x4 w = philox4x32_10(u32x4{uint32_t(site[v]), gstep, kStreamWiener, 0u}, seed, id);
+          xi_lo = normal_pair(w.x, w.y, R(0));
+          xi_hi = normal_pair(w.z, w.w, R(0));
+        } else {
+          const T* nz = noise_tr + int64_t(gstep) * N;
+          xi_lo = nz[site[v]];
+          xi_hi = valid[v + H] ? nz[site[v + H]] : cmake<T>(R(0), R(0));
+        }
+        beta[v] = local_update(beta[v], h[v], rsl[v], iU[v], iF[v], dt, dt4, xi_lo);
+        beta[v + H] = local_update(beta[v + H], h[v + H], rsl[v + H], iU[v + H], iF[v + H], dt, dt4, xi_hi);
+      }
+    }
+    if (active) {
+      bool bad = false;
+#pragma unroll
+      for (int v = 0; v < VPT; ++v) if (valid[v]) { st[site[v]] = beta[v]; bad |= !finite_c(beta[v]); }
+      set_status(a.status, traj, bad);
+    }
+  }
+}
+
+}  // namespace twmc

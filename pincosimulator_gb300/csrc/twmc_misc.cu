@@ -1,0 +1,200 @@
+// twmc_misc.cu -- one-off kernels: initial fields and disorder draws (FP64,
+// Philox streams), the FP64 ensemble reduction, and the Philox self-check.
+#include <algorithm>
+
+#include "twmc_common.cuh"
+#include "twmc_launch.h"
+
+namespace twmc {
+
+namespace {
+
+__device__ __forceinline__ double2 ld_c(const double* p, int64_t i) { return make_double2(p[2 * i], p[2 * i + 1]); }
+
+// One trajectory-site of the initial state (TWMCBaseSolver.cpp:126-151 /
+// TWMCLiebSolver.cpp:145-171 with the noise drawn from Philox streams).
+__global__ void init_kernel(const InitArgs a) {
+  const int64_t total = a.ntraj * a.nsites;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t tr = i / a.nsites, p = i % a.nsites;
+    const uint32_t seed = a.seeds[tr], id = a.ids[tr];
+    int hi;
+    const uint32_t c0 = site_ctr(p, a.nsites, &hi);
+    double2 b;
+    if (a.ic_kind == 2) {
+      b = ld_c(a.given, i);
+    } else {
+      b = a.binit ? ld_c(a.binit, p) : make_double2(0.0, 0.0);
+      if (a.ic_kind == 0) {
+        const u32x4 w = philox4x32_10(u32x4{c0, 0u, kStreamInit, 0u}, seed, id);
+        const double2 z = hi ? normal_pair(w.z, w.w, 0.0) : normal_pair(w.x, w.y, 0.0);
+        const double2 sg = a.bsigma ? ld_c(a.bsigma, p) : make_double2(0.0, 0.0);
+        b = cadd(b, cmul(sg, z));
+      }
+    }
+    double2 v[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+      if (a.given_real[m]) {
+        v[m] = ld_c(a.given_real[m], i);
+        continue;
+      }
+      v[m] = a.base[m] ? ld_c(a.base[m], p) : make_double2(0.0, 0.0);
+      if (a.kind[m] != 0) {
+        const u32x4 w = philox4x32_10(u32x4{c0, 0u, a.stream[m], 0u}, seed, id);
+        const double2 amp = ld_c(a.amp[m], p);
+        if (a.kind[m] == 1) {
+          const double2 z = hi ? normal_pair(w.z, w.w, 0.0) : normal_pair(w.x, w.y, 0.0);
+          v[m].x += z.x * amp.x;
+          v[m].y += z.y * amp.y;
+        } else {
+          const uint32_t u0 = hi ? w.z : w.x, u1 = hi ? w.w : w.y;
+          v[m].x += double(u0) * 0x1p-32 * amp.x;
+          v[m].y += double(u1) * 0x1p-32 * amp.y;
+        }
+      }
+    }
+#pragma unroll
+    for (int m = 0; m < 3; ++m)
+      if (a.real_out[m]) { a.real_out[m][2 * i] = v[m].x; a.real_out[m][2 * i + 1] = v[m].y; }
+    // v[0] = U, v[1] = omega (Lieb: E), v[2] = F
+    double2 rsl;
+    if (a.lattice == 0) rsl = make_double2(v[1].y - a.gamma / 2.0, -v[1].x);     // -i omega - gamma/2
+    else {
+      const double2 d = make_double2(a.detuning - v[1].x, -v[1].y);            // detuning - E
+      rsl = make_double2(d.y - a.gamma / 2.0, -d.x);                            // -i delta - gamma/2
+    }
+    const double2 iU = make_double2(-v[0].y, v[0].x);
+    const double2 iF = make_double2(-v[2].y, v[2].x);
+    if (a.prec == 0) {
+      reinterpret_cast<float2*>(a.state)[i] = make_float2(float(b.x), float(b.y));
+      if (a.rsl) reinterpret_cast<float2*>(a.rsl)[i] = make_float2(float(rsl.x), float(rsl.y));
+      if (a.iU) reinterpret_cast<float2*>(a.iU)[i] = make_float2(float(iU.x), float(iU.y));
+      if (a.iF) reinterpret_cast<float2*>(a.iF)[i] = make_float2(float(iF.x), float(iF.y));
+    } else {
+      reinterpret_cast<double2*>(a.state)[i] = b;
+      if (a.rsl) reinterpret_cast<double2*>(a.rsl)[i] = rsl;
+      if (a.iU) reinterpret_cast<double2*>(a.iU)[i] = iU;
+      if (a.iF) reinterpret_cast<double2*>(a.iF)[i] = iF;
+    }
+  }
+}
+
+// Neumaier-compensated FP64 accumulator.
+struct KSum {
+  double s = 0.0, c = 0.0;
+  __device__ __forceinline__ void add(double x) {
+    const double t = s + x;
+    c += (fabs(s) >= fabs(x)) ? ((s - t) + x) : ((x - t) + s);
+    s = t;
+  }
+  __device__ __forceinline__ double value() const { return s + c; }
+};
+
+// Ensemble sums over trajectory block b = [b T / B, (b+1) T / B), in
+// trajectory order: sum |a|^2, sum |a|^4, sum |a_k|^2. One thread per
+// (block, site); deterministic for a given (T, B).
+template <typename R>
+__global__ void moments_kernel(const MomentArgs a) {
+  using T = c2_t<R>;
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  const int b = blockIdx.y;
+  if (p >= a.nsites) return;
+  const int64_t t0 = (int64_t(b) * a.ntraj) / a.nblocks, t1 = (int64_t(b + 1) * a.ntraj) / a.nblocks;
+  KSum s2, s4, sk;
+  const T* st = reinterpret_cast<const T*>(a.state);
+  const R* nk = reinterpret_cast<const R*>(a.nk);
+  for (int64_t tr = t0; tr < t1; ++tr) {
+    const T v = st[tr * a.nsites + p];
+    const double ab2 = double(v.x) * double(v.x) + double(v.y) * double(v.y);
+    s2.add(ab2);
+    s4.add(ab2 * ab2);
+    if (nk) sk.add(double(nk[tr * a.nsites + p]));
+  }
+  double* o = a.out + (int64_t(b) * a.nsites + p) * 3;
+  o[0] = s2.value();
+  o[1] = s4.value();
+  o[2] = sk.value();
+}
+
+__global__ void philox_kernel(const uint32_t* ctr, size_t n, uint32_t k0, uint32_t k1, uint32_t* out) {
+  const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
+  if (i >= n) return;
+  const u32x4 r = philox4x32_10(u32x4{ctr[4 * i], ctr[4 * i + 1], ctr[4 * i + 2], ctr[4 * i + 3]}, k0, k1);
+  out[4 * i] = r.x; out[4 * i + 1] = r.y; out[4 * i + 2] = r.z; out[4 * i + 3] = r.w;
+}
+
+// 8 independent FMA chains per thread; 2 flops per FMA.
+__global__ void fma_kernel(float* out, int iters, float a, float b) {
+  float x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = float(threadIdx.x + k);
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) x[k] = fmaf(x[k], a, b);
+  }
+  float s = 0.f;
+#pragma unroll
+  for (int k = 0; k < 8; ++k) s += x[k];
+  if (s == 1.2345f) out[0] = s;  // keeps the chains alive
+}
+
+bool check(cudaError_t e, std::string* err, const char* what) {
+  if (e == cudaSuccess) return true;
+  if (err) *err = std::string(what) + ": " + cudaGetErrorString(e);
+  return false;
+}
+
+}  // namespace
+
+bool init_launch(const InitArgs& a, cudaStream_t s, std::string* err) {
+  const int64_t total = a.ntraj * a.nsites;
+  if (total <= 0) return true;
+  const int64_t blocks = std::min<int64_t>((total + 255) / 256, 152 * 32);
+  init_kernel<<<int(blocks), 256, 0, s>>>(a);
+  return check(cudaGetLastError(), err, "init_kernel");
+}
+
+bool moments_launch(const MomentArgs& a, cudaStream_t s, std::string* err) {
+  dim3 grid(unsigned((a.nsites + 127) / 128), unsigned(a.nblocks));
+  if (a.prec == 0) moments_kernel<float><<<grid, 128, 0, s>>>(a);
+  else moments_kernel<double><<<grid, 128, 0, s>>>(a);
+  return check(cudaGetLastError(), err, "moments_kernel");
+}
+
+bool fp32_peak(double* tflops, std::string* err) {
+  int dev = 0, sms = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  float* out = nullptr;
+  if (!check(cudaMalloc(&out, sizeof(float)), err, "fp32 peak alloc")) return false;
+  const int threads = 512, blocks = sms * 4, iters = 1 << 16;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 0.0;
+  for (int rep = 0; rep < 6; ++rep) {
+    cudaEventRecord(e0);
+    fma_kernel<<<blocks, threads>>>(out, iters, 0.999999f, 1e-7f);
+    cudaEventRecord(e1);
+    if (!check(cudaEventSynchronize(e1), err, "fp32 peak")) break;
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double flops = 2.0 * 8.0 * double(iters) * double(threads) * double(blocks);
+    if (rep > 0 && ms > 0) best = std::max(best, flops / (double(ms) * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  *tflops = best;
+  return best > 0.0;
+}
+
+bool philox_launch(const uint32_t* d_ctr, size_t n, uint32_t k0, uint32_t k1, uint32_t* d_out, cudaStream_t s,
+                   std::string* err) {
+  if (n == 0) return true;
+  philox_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(d_ctr, n, k0, k1, d_out);
+  return check(cudaGetLastError(), err, "philox_kernel");
+}
+
+}  // namespace twmc

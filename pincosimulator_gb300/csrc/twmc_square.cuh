@@ -1,0 +1,85 @@
+// twmc_square.cuh -- launcher of the square-lattice FFT step kernel for the
+// compiled shapes (one translation unit per precision).
+#pragma once
+
+#include <algorithm>
+#include <string>
+
+#include "fft_plans.inc"
+#include "twmc_kernels.cuh"
+#include "twmc_launch.h"
+
+namespace twmc {
+
+// Threads per CTA: whole trajectories, up to 256 threads, with the exchange
+// buffers and up to three per-site parameter slices of all trajectories of
+// the CTA inside a ~100 KB shared-memory budget.
+template <typename R, class P>
+constexpr int cta_for() {
+  constexpr int tpt = PlanInfo<P>::TPT;
+  constexpr size_t per_traj = 5 * sizeof(c2_t<R>) * size_t(PlanInfo<P>::N);
+  int tpc = tpt >= 256 ? 1 : 256 / tpt;
+  while (tpc > 1 && size_t(tpc) * per_traj > 100 * 1024) tpc /= 2;
+  return tpc * tpt;
+}
+
+template <typename R, class P>
+bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo* info, std::string* err) {
+  constexpr int CTA = cta_for<R, P>();
+  using Cfg = SquareCfg<P, CTA>;
+  int dev0 = 0, maxsm = 0;
+  cudaGetDevice(&dev0);
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev0);
+  StepArgs a2 = a;
+  size_t smem = Cfg::template smem_bytes<R>(nparams);
+  a2.dbuf = 1;  // parameters in shared memory
+  if (nparams > 0 && smem > size_t(maxsm) / 2) {
+    smem = Cfg::template smem_bytes<R>(0);
+    a2.dbuf = 0;  // parameters read from global memory
+  }
+  auto fn = square_fft_kernel<R, P, CTA>;
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) {
+    if (err) *err = std::string("square kernel smem attribute: ") + cudaGetErrorString(e);
+    return false;
+  }
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, CTA, smem);
+  if (e != cudaSuccess || per_sm <= 0) {
+    if (err) *err = std::string("square kernel does not fit on an SM (smem ") + std::to_string(smem) + " B)";
+    return false;
+  }
+  const int64_t groups = (a.ntraj + Cfg::TPC - 1) / Cfg::TPC;
+  const int grid = int(std::min<int64_t>(groups, int64_t(sms) * per_sm));
+  if (info) {
+    info->name = "square_fft_kernel";
+    info->cta = CTA;
+    info->grid = grid;
+    info->smem = smem;
+    info->blocks_per_sm = per_sm;
+  }
+  if (grid <= 0) return true;
+  fn<<<grid, CTA, smem, s>>>(a2);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    if (err) *err = std::string("square kernel launch: ") + cudaGetErrorString(e);
+    return false;
+  }
+  return true;
+}
+
+template <typename R>
+bool square_dispatch(int bx, int by, const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo* info,
+                     std::string* err) {
+#define TWMC_SHAPE(BX, BY) \
+  if (bx == BX && by == BY) return square_launch_t<R, Plan_##BX##_##BY>(a, nparams, s, info, err);
+  TWMC_SHAPE(0, 5) TWMC_SHAPE(0, 6) TWMC_SHAPE(0, 7) TWMC_SHAPE(0, 8) TWMC_SHAPE(0, 9) TWMC_SHAPE(0, 10)
+  TWMC_SHAPE(0, 11) TWMC_SHAPE(0, 12) TWMC_SHAPE(4, 4) TWMC_SHAPE(5, 5) TWMC_SHAPE(6, 6)
+#undef TWMC_SHAPE
+  if (err) *err = "square FFT kernel not compiled for this shape";
+  return false;
+}
+
+}  // namespace twmc

@@ -1,0 +1,303 @@
+"""ctypes binding of libtwmc_cuda.so (include/twmc.h).
+
+This is the Python-side caller of the C ABI, the same boundary a C++
+Solver plugin or any FFI binds. There is no CPU fallback: constructing a
+`System` without the compiled library, or without a CUDA device, raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass
+from typing import Optional, Sequence
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libtwmc_cuda.so")
+
+# enums (twmc.h)
+OK, ERR_INVALID, ERR_CUDA, ERR_TIMEOUT, ERR_NONFINITE, ERR_NOMEM, ERR_NOT_BUILT = 0, -1, -2, -3, -4, -5, -6
+LATTICE_SQUARE, LATTICE_LIEB = 0, 1
+PREC_F32, PREC_F64 = 0, 1
+NOISE_PHILOX, NOISE_BUFFER = 0, 1
+HOP_FFT, HOP_STENCIL = 0, 1
+IC_SETTINGS, IC_FIXED, IC_GIVEN = 0, 1, 2
+DISORDER_NONE, DISORDER_GAUSSIAN, DISORDER_UNIFORM = 0, 1, 2
+
+EXPORTED = [
+    "twmc_version", "twmc_create", "twmc_run", "twmc_set_noise_buffer", "twmc_progress", "twmc_last_error",
+    "twmc_destroy", "twmc_batch_init", "twmc_batch_advance", "twmc_batch_reduce", "twmc_sync",
+    "twmc_batch_download", "twmc_launch_count", "twmc_kernel_name", "twmc_stream", "twmc_measure_fp32_peak",
+    "twmc_debug_philox",
+]
+
+
+class Matrix(C.Structure):
+    _fields_ = [("base", C.c_void_p), ("noise_kind", C.c_int32), ("noise_amp", C.c_void_p)]
+
+
+class SystemDesc(C.Structure):
+    _fields_ = [
+        ("lattice", C.c_int32), ("nx", C.c_int64), ("ny", C.c_int64), ("pbc", C.c_int32),
+        ("J", C.c_double), ("J_AB", C.c_double), ("J_BC", C.c_double), ("gamma", C.c_double),
+        ("detuning", C.c_double), ("dt", C.c_double), ("frame_steps", C.c_int64),
+        ("omega", Matrix), ("U", Matrix), ("F", Matrix), ("beta_init", Matrix), ("beta_init_sigma", Matrix),
+        ("ft_nrec", C.c_int64), ("ft_times", C.c_void_p), ("ft_values", C.c_void_p),
+        ("precision", C.c_int32), ("noise_mode", C.c_int32), ("hop_mode", C.c_int32), ("n_moment_blocks", C.c_int32),
+    ]
+
+
+class TaskDesc(C.Structure):
+    _fields_ = [
+        ("id", C.c_uint64), ("seed", C.c_uint32), ("ic_kind", C.c_int32), ("t_start", C.c_double),
+        ("t_end", C.c_double), ("store_initial", C.c_int32), ("init_field", C.c_void_p),
+        ("U_realization", C.c_void_p), ("omega_realization", C.c_void_p), ("F_realization", C.c_void_p),
+    ]
+
+
+class Outputs(C.Structure):
+    _fields_ = [
+        ("frames", C.c_void_p), ("final_field", C.c_void_p), ("U_realization", C.c_void_p),
+        ("omega_realization", C.c_void_p), ("F_realization", C.c_void_p), ("moments", C.c_void_p),
+        ("frames_written", C.c_void_p), ("t_final", C.c_void_p), ("status", C.c_void_p),
+    ]
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads the C-ABI library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"libtwmc_cuda.so not built ({path}); run __graft_entry__.build()")
+    lib = C.CDLL(path)
+    lib.twmc_version.restype = C.c_int
+    lib.twmc_create.argtypes = [C.POINTER(SystemDesc), C.POINTER(C.c_void_p)]
+    lib.twmc_run.argtypes = [C.c_void_p, C.POINTER(TaskDesc), C.c_size_t, C.POINTER(Outputs)]
+    lib.twmc_set_noise_buffer.argtypes = [C.c_void_p, C.c_void_p, C.c_size_t]
+    lib.twmc_progress.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    lib.twmc_last_error.argtypes = [C.c_void_p]
+    lib.twmc_last_error.restype = C.c_char_p
+    lib.twmc_destroy.argtypes = [C.c_void_p]
+    lib.twmc_destroy.restype = None
+    lib.twmc_batch_init.argtypes = [C.c_void_p, C.POINTER(TaskDesc), C.c_size_t]
+    lib.twmc_batch_advance.argtypes = [C.c_void_p, C.c_int64]
+    lib.twmc_batch_reduce.argtypes = [C.c_void_p]
+    lib.twmc_sync.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    lib.twmc_batch_download.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.twmc_launch_count.argtypes = [C.c_void_p]
+    lib.twmc_launch_count.restype = C.c_int64
+    lib.twmc_kernel_name.argtypes = [C.c_void_p]
+    lib.twmc_kernel_name.restype = C.c_char_p
+    lib.twmc_debug_philox.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]
+    lib.twmc_stream.argtypes = [C.c_void_p]
+    lib.twmc_stream.restype = C.c_void_p
+    lib.twmc_measure_fp32_peak.argtypes = [C.POINTER(C.c_double)]
+    _lib = lib
+    return lib
+
+
+class TWMCError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"twmc error {code}: {msg}")
+        self.code = code
+
+
+def _cplx(v, n: int) -> np.ndarray:
+    a = np.asarray(v, dtype=np.complex128)
+    if a.ndim == 0:
+        a = np.full(n, complex(a), dtype=np.complex128)
+    a = np.ascontiguousarray(a.reshape(-1))
+    if a.size != n:
+        raise ValueError(f"expected {n} values, got {a.size}")
+    return a
+
+
+def _ptr(a: Optional[np.ndarray]):
+    return None if a is None else a.ctypes.data
+
+
+@dataclass
+class Noisy:
+    """A parameter matrix: base value(s) plus an optional per-trajectory disorder draw."""
+    base: object = 0.0
+    kind: int = DISORDER_NONE
+    amp: object = 0.0
+
+
+class System:
+    """One lattice system (the reference's TWMCSystemData + solver Setup)."""
+
+    def __init__(self, *, lattice=LATTICE_SQUARE, nx=1, ny=1, pbc=True, J=0.0, J_AB=0.0, J_BC=0.0, gamma=1.0,
+                 detuning=0.0, dt=0.01, frame_steps=1, omega=0.0, U=0.0, F=0.0, beta_init=0.0, beta_init_sigma=0.0,
+                 F_t: Optional[tuple] = None, precision=PREC_F32, noise=NOISE_PHILOX, hop=HOP_FFT, n_moment_blocks=32):
+        self.lib = load()
+        self.n_sites = (3 if lattice == LATTICE_LIEB else 1) * nx * ny
+        n = self.n_sites
+        self._keep = []
+        d = SystemDesc()
+        d.lattice, d.nx, d.ny, d.pbc = lattice, nx, ny, int(bool(pbc))
+        d.J, d.J_AB, d.J_BC, d.gamma, d.detuning, d.dt = J, J_AB, J_BC, gamma, detuning, dt
+        d.frame_steps = frame_steps
+        for name, val in (("omega", omega), ("U", U), ("F", F), ("beta_init", beta_init),
+                          ("beta_init_sigma", beta_init_sigma)):
+            nv = val if isinstance(val, Noisy) else Noisy(base=val)
+            base = _cplx(nv.base, n)
+            amp = _cplx(nv.amp, n)
+            self._keep += [base, amp]
+            setattr(d, name, Matrix(base.ctypes.data, nv.kind, amp.ctypes.data if nv.kind else None))
+        if F_t is not None:
+            times, vals = F_t
+            times = np.ascontiguousarray(np.asarray(times, dtype=np.float64))
+            vals = np.ascontiguousarray(np.asarray(vals, dtype=np.complex128).reshape(len(times), n))
+            self._keep += [times, vals]
+            d.ft_nrec, d.ft_times, d.ft_values = len(times), times.ctypes.data, vals.ctypes.data
+        d.precision, d.noise_mode, d.hop_mode, d.n_moment_blocks = precision, noise, hop, n_moment_blocks
+        self.desc = d
+        self.n_blocks = n_moment_blocks
+        self.precision = precision
+        h = C.c_void_p()
+        rc = self.lib.twmc_create(C.byref(d), C.byref(h))
+        self.h = h
+        if rc != OK:
+            msg = self.last_error()
+            self.close()
+            raise TWMCError(rc, msg)
+
+    # -- plumbing --------------------------------------------------------
+    def last_error(self) -> str:
+        if not self.h:
+            return ""
+        return self.lib.twmc_last_error(self.h).decode()
+
+    def _check(self, rc: int):
+        if rc != OK:
+            raise TWMCError(rc, self.last_error())
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.twmc_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def kernel_name(self) -> str:
+        return self.lib.twmc_kernel_name(self.h).decode()
+
+    @property
+    def stream(self) -> int:
+        """cudaStream_t of the handle (an integer address)."""
+        return int(self.lib.twmc_stream(self.h) or 0)
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.twmc_launch_count(self.h))
+
+    # -- tasks -----------------------------------------------------------
+    def make_tasks(self, n: int, *, t_start=0.0, t_end=1.0, seed0=1234, id0=1, store_initial=True,
+                   ic=IC_SETTINGS, init_field=None, seeds: Optional[Sequence[int]] = None):
+        tasks = (TaskDesc * n)()
+        keep = []
+        if init_field is not None:
+            f = np.ascontiguousarray(np.asarray(init_field, dtype=np.complex128).reshape(n, self.n_sites))
+            keep.append(f)
+        for i in range(n):
+            t = tasks[i]
+            t.id = id0 + i
+            t.seed = (seeds[i] if seeds is not None else seed0 + i) & 0xFFFFFFFF
+            t.ic_kind = ic
+            t.t_start, t.t_end = t_start, t_end
+            t.store_initial = int(bool(store_initial))
+            if init_field is not None:
+                t.init_field = f[i].ctypes.data
+        self._keep.append(keep)
+        return tasks
+
+    def set_noise(self, xi: np.ndarray):
+        """Deterministic-noise mode: xi[task][step][site] complex normals."""
+        xi = np.ascontiguousarray(np.asarray(xi, dtype=np.complex128))
+        self._noise = xi
+        self._check(self.lib.twmc_set_noise_buffer(self.h, xi.ctypes.data, xi.size))
+
+    def run(self, tasks, *, frames=True, final=True, moments=False, realizations=False, n_frames=None):
+        """twmc_run: returns a dict of numpy arrays."""
+        n = len(tasks)
+        N = self.n_sites
+        if n_frames is None:
+            dt_obs = self.desc.dt * self.desc.frame_steps
+            n_frames = max(int(round((t.t_end - t.t_start) / dt_obs)) + int(t.store_initial) for t in tasks)
+        out = Outputs()
+        res = {}
+        if frames:
+            res["frames"] = np.zeros((n, n_frames, N), dtype=np.complex128)
+            out.frames = res["frames"].ctypes.data
+        if final:
+            res["final"] = np.zeros((n, N), dtype=np.complex128)
+            out.final_field = res["final"].ctypes.data
+        if moments:
+            res["moments"] = np.zeros((n_frames, self.n_blocks, N, 3), dtype=np.float64)
+            out.moments = res["moments"].ctypes.data
+        if realizations:
+            for key in ("U_realization", "omega_realization", "F_realization"):
+                res[key] = np.zeros((n, N), dtype=np.complex128)
+                setattr(out, key, res[key].ctypes.data)
+        res["frames_written"] = np.zeros(n, dtype=np.int64)
+        res["t_final"] = np.zeros(n, dtype=np.float64)
+        res["status"] = np.zeros(n, dtype=np.int32)
+        out.frames_written = res["frames_written"].ctypes.data
+        out.t_final = res["t_final"].ctypes.data
+        out.status = res["status"].ctypes.data
+        self._check(self.lib.twmc_run(self.h, tasks, n, C.byref(out)))
+        return res
+
+    # -- device-resident batch API ---------------------------------------
+    def batch_init(self, tasks):
+        self._check(self.lib.twmc_batch_init(self.h, tasks, len(tasks)))
+        self._batch_n = len(tasks)
+
+    def advance(self, n_steps: int):
+        self._check(self.lib.twmc_batch_advance(self.h, int(n_steps)))
+
+    def reduce(self):
+        self._check(self.lib.twmc_batch_reduce(self.h))
+
+    def sync(self) -> float:
+        ms = C.c_double()
+        self._check(self.lib.twmc_sync(self.h, C.byref(ms)))
+        return ms.value
+
+    def download(self, field=True, moments=False):
+        f = np.zeros((self._batch_n, self.n_sites), dtype=np.complex128) if field else None
+        m = np.zeros((self.n_blocks, self.n_sites, 3), dtype=np.float64) if moments else None
+        self._check(self.lib.twmc_batch_download(self.h, _ptr(f), _ptr(m)))
+        return f, m
+
+
+def measure_fp32_peak() -> float:
+    """Measured FP32 FMA throughput of the current device (TFLOP/s)."""
+    lib = load()
+    v = C.c_double()
+    rc = lib.twmc_measure_fp32_peak(C.byref(v))
+    if rc != OK:
+        raise TWMCError(rc, "FP32 peak measurement failed")
+    return v.value
+
+
+def debug_philox(ctr: np.ndarray, key) -> np.ndarray:
+    lib = load()
+    ctr = np.ascontiguousarray(np.asarray(ctr, dtype=np.uint32).reshape(-1, 4))
+    k = np.ascontiguousarray(np.asarray(key, dtype=np.uint32).reshape(2))
+    out = np.zeros_like(ctr)
+    rc = lib.twmc_debug_philox(ctr.ctypes.data, ctr.shape[0], k.ctypes.data, out.ctypes.data)
+    if rc != OK:
+        raise TWMCError(rc, "twmc_debug_philox failed")
+    return out

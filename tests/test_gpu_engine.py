@@ -1,0 +1,164 @@
+"""GPU checks of the engine beyond single-trajectory parity: Philox noise,
+initial fields and disorder, ensemble moments, status flags, full-size
+properties."""
+import numpy as np
+import pytest
+
+from oracle import twmc_oracle as npo
+from pincosimulator_gb300 import twmc
+
+from gpu_util import rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+def test_gpu_philox_bit_exact(built_lib, oracle):
+    rng = np.random.default_rng(2)
+    ctr = rng.integers(0, 2**32, size=(4096, 4), dtype=np.uint64).astype(np.uint32)
+    key = [0x9E3779B9, 0x7F4A7C15]
+    assert np.array_equal(twmc.debug_philox(ctr, key), npo.philox4x32_10(ctr, np.broadcast_to(np.array(key, np.uint32), (4096, 2))))
+
+
+@pytest.mark.parametrize("prec,noise,tol", [(twmc.PREC_F64, "philox64", 1e-12), (twmc.PREC_F32, "philox32", 1e-4)])
+@pytest.mark.parametrize("shape,hop", [((16, 16), twmc.HOP_FFT), ((1, 64), twmc.HOP_FFT), ((6, 10), twmc.HOP_STENCIL)])
+def test_philox_noise_trajectories(built_lib, oracle, prec, noise, tol, shape, hop):
+    nx, ny = shape
+    n = nx * ny
+    ntraj, steps, dt = 3, 200, 0.005
+    rng = np.random.default_rng(3)
+    beta0 = 0.3 * (rng.normal(size=(ntraj, n)) + 1j * rng.normal(size=(ntraj, n)))
+    sysd = twmc.System(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=dt, frame_steps=50, omega=-0.5, U=0.2, F=1.5,
+                       precision=prec, noise=twmc.NOISE_PHILOX, hop=hop)
+    seeds = [17, 99, 12345]
+    tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=steps * dt, ic=twmc.IC_GIVEN, init_field=beta0, seeds=seeds,
+                            id0=5)
+    res = sysd.run(tasks, frames=False)
+    sysd.close()
+    for k in range(ntraj):
+        ref = oracle.base_run(nx, ny, 1.0, 1.0, dt, 0.0, steps * dt, 50, 5, True, -0.5, 0.2, 1.5, beta0[k],
+                              seed=seeds[k], tid=5 + k, noise=noise)
+        assert rel_err(res["final"][k], ref["final"]) < tol
+
+
+def test_initial_fields_and_disorder(built_lib, oracle):
+    """ReadFromSettings initial fields and Gaussian / Uniform disorder draws (FP64 state)."""
+    nx, ny, ntraj = 8, 8, 4
+    n = nx * ny
+    rng = np.random.default_rng(8)
+    binit = 0.2 + 0.1j * rng.normal(size=n)
+    bsig = 0.5 + 0.1 * rng.random(size=n)
+    om_amp = 0.2 + 0.05j
+    u_amp = 0.06 * np.ones(n)
+    f_amp = 1.0 + 0.5j
+    sysd = twmc.System(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=0.01, frame_steps=1,
+                       omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, om_amp),
+                       U=twmc.Noisy(0.27, twmc.DISORDER_UNIFORM, u_amp),
+                       F=twmc.Noisy(2.0, twmc.DISORDER_GAUSSIAN, f_amp),
+                       beta_init=binit, beta_init_sigma=bsig, precision=twmc.PREC_F64)
+    tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=0.01, seed0=77, id0=3)
+    res = sysd.run(tasks, frames=True, realizations=True)
+    sysd.close()
+    for k in range(ntraj):
+        seed, tid = 77 + k, 3 + k
+        assert rel_err(res["frames"][k, 0], oracle.initial_field(n, binit, bsig, seed, tid)) < 1e-14
+        assert rel_err(res["U_realization"][k], oracle.disorder(n, 2, 0.27, u_amp, seed, tid, 2)) < 1e-14
+        assert rel_err(res["omega_realization"][k], oracle.disorder(n, 1, -0.5, om_amp, seed, tid, 3)) < 1e-14
+        assert rel_err(res["F_realization"][k], oracle.disorder(n, 1, 2.0, f_amp, seed, tid, 4)) < 1e-14
+
+
+def test_disordered_trajectories_match_oracle(built_lib, oracle):
+    """C2-style omega disorder: the drawn realisation drives the trajectory (FP64, Philox)."""
+    nx = ny = 16
+    n = nx * ny
+    ntraj, steps, dt = 3, 100, 0.002
+    sysd = twmc.System(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=dt, frame_steps=50,
+                       omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=0.2, F=2.0, beta_init=0.0,
+                       beta_init_sigma=0.5, precision=twmc.PREC_F64)
+    tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=steps * dt, seed0=5, id0=1)
+    res = sysd.run(tasks, frames=True, realizations=True)
+    sysd.close()
+    for k in range(ntraj):
+        b0 = res["frames"][k, 0]
+        ref = oracle.base_run(nx, ny, 1.0, 1.0, dt, 0.0, steps * dt, 50, 3, True, res["omega_realization"][k], 0.2,
+                              2.0, b0, seed=5 + k, tid=1 + k, noise="philox64")
+        assert rel_err(res["final"][k], ref["final"]) < 1e-12
+
+
+def test_moments_match_frames(built_lib, oracle):
+    nx = ny = 16
+    n = nx * ny
+    ntraj, nb = 40, 8
+    sysd = twmc.System(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=0.005, frame_steps=20, omega=-0.5, U=0.2, F=1.0,
+                       beta_init_sigma=0.5, precision=twmc.PREC_F64, n_moment_blocks=nb)
+    tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=0.2, seed0=1)
+    res = sysd.run(tasks, frames=True, moments=True)
+    sysd.close()
+    fr = res["frames"]  # (T, F, N)
+    for f in range(fr.shape[1]):
+        for b in range(nb):
+            t0, t1 = b * ntraj // nb, (b + 1) * ntraj // nb
+            x = fr[t0:t1, f]
+            ab2 = np.abs(x) ** 2
+            fk = np.fft.fft2(x.reshape(-1, nx, ny)).reshape(-1, n) / np.sqrt(n)
+            assert np.allclose(res["moments"][f, b, :, 0], ab2.sum(0), rtol=1e-12, atol=1e-12)
+            assert np.allclose(res["moments"][f, b, :, 1], (ab2 ** 2).sum(0), rtol=1e-12, atol=1e-12)
+            # n_k is stored at natural k order
+            assert np.allclose(res["moments"][f, b, :, 2], (np.abs(fk) ** 2).sum(0), rtol=1e-10, atol=1e-10)
+
+
+def test_nonfinite_status_flag(built_lib):
+    """A NaN injected into one trajectory's host noise is reported in its status only."""
+    nx = ny = 16
+    n = nx * ny
+    ntraj, steps, dt = 3, 20, 0.01
+    xi = np.zeros((ntraj, steps, n), dtype=complex)
+    xi[1, 7, 5] = np.nan
+    sysd = twmc.System(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=dt, frame_steps=10, omega=0.0, U=0.1, F=0.5,
+                       noise=twmc.NOISE_BUFFER)
+    tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=steps * dt, ic=twmc.IC_GIVEN,
+                            init_field=np.zeros((ntraj, n)))
+    sysd.set_noise(xi)
+    res = sysd.run(tasks, frames=False)
+    sysd.close()
+    assert list(res["status"]) == [0, twmc.ERR_NONFINITE, 0]
+
+
+def test_invalid_arguments_rejected(built_lib):
+    with pytest.raises(twmc.TWMCError):
+        twmc.System(nx=0, ny=4)
+    with pytest.raises(twmc.TWMCError):
+        twmc.System(lattice=twmc.LATTICE_LIEB, nx=4, ny=4)
+    sysd = twmc.System(nx=4, ny=4, dt=0.01, noise=twmc.NOISE_BUFFER)
+    tasks = sysd.make_tasks(2, t_end=0.1, ic=twmc.IC_GIVEN, init_field=np.zeros((2, 16)))
+    with pytest.raises(twmc.TWMCError):
+        sysd.run(tasks)  # no noise buffer supplied
+    sysd.set_noise(np.zeros((2, 3, 16)))
+    with pytest.raises(twmc.TWMCError):
+        sysd.run(tasks)  # too short
+    sysd.close()
+
+
+def test_full_size_fft_equals_stencil(built_lib):
+    """C2 size (16384 trajectories of 64 x 64, FP32, Philox): the k-space
+    (FFT) and real-space kernels apply the same operator; after 50 steps the
+    fields agree to FP32 rounding, and the FP64 moment blocks sum to the
+    downloaded fields' moments."""
+    nx = ny = 64
+    ntraj = 16384
+    kw = dict(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=0.002, frame_steps=250, U=0.2, F=2.0,
+              omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), beta_init_sigma=0.5, precision=twmc.PREC_F32)
+    out = {}
+    for hop in (twmc.HOP_FFT, twmc.HOP_STENCIL):
+        sysd = twmc.System(hop=hop, **kw)
+        tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=100.0, seed0=2024)
+        sysd.batch_init(tasks)
+        sysd.advance(50)
+        sysd.reduce()
+        sysd.sync()
+        out[hop] = sysd.download(field=True, moments=True)
+        sysd.close()
+    fa, ma = out[twmc.HOP_FFT]
+    fb, mb = out[twmc.HOP_STENCIL]
+    assert np.isfinite(fa).all()
+    assert rel_err(fa, fb) < 1e-4
+    assert np.allclose(ma[:, :, 0].sum(0), (np.abs(fa) ** 2).sum(0), rtol=1e-9)

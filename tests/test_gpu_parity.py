@@ -1,0 +1,76 @@
+"""GPU parity against the oracle through the C ABI (deterministic-noise mode).
+
+Tolerances: FP32 state/FFT 1e-5 normwise relative, FP64 mode 1e-12, on
+short horizons (200 Euler steps), as the deterministic-noise criterion
+states.
+"""
+import numpy as np
+import pytest
+
+from pincosimulator_gb300 import twmc
+
+from gpu_util import check, lieb_case, square_case
+
+pytestmark = pytest.mark.gpu
+
+FFT_SHAPES = [(1, 32), (1, 64), (1, 128), (1, 256), (1, 512), (1, 1024), (1, 2048), (1, 4096), (16, 16), (32, 32),
+              (64, 64)]
+
+
+@pytest.mark.parametrize("prec", [twmc.PREC_F32, twmc.PREC_F64])
+@pytest.mark.parametrize("shape", FFT_SHAPES)
+def test_square_fft_parity(built_lib, oracle, shape, prec):
+    nx, ny = shape
+    ntraj = 2 if nx * ny >= 4096 else 5
+    res, refs = square_case(oracle, nx, ny, ntraj=ntraj, prec=prec)
+    assert res["kernel"] == "square_fft_kernel"
+    check(res, refs, prec)
+
+
+@pytest.mark.parametrize("prec", [twmc.PREC_F32, twmc.PREC_F64])
+@pytest.mark.parametrize("shape", [(1, 1), (1, 2), (2, 2), (1, 50), (6, 10), (4, 8), (64, 64), (1, 64), (3, 128)])
+def test_square_stencil_parity(built_lib, oracle, shape, prec):
+    nx, ny = shape
+    res, refs = square_case(oracle, nx, ny, ntraj=3, prec=prec, hop=twmc.HOP_STENCIL)
+    assert res["kernel"].startswith("ell_kernel")
+    check(res, refs, prec)
+
+
+def test_nonpow2_falls_back_to_real_space(built_lib, oracle):
+    res, refs = square_case(oracle, 6, 10, ntraj=2, prec=twmc.PREC_F32, hop=twmc.HOP_FFT)
+    assert res["kernel"] == "ell_kernel<stencil>"
+    check(res, refs, twmc.PREC_F32)
+
+
+def test_per_site_parameters(built_lib, oracle):
+    rng = np.random.default_rng(5)
+    n = 32 * 32
+    omega = -0.5 + 0.2 * rng.normal(size=n)
+    U = 0.2 + 0.02j * rng.normal(size=n)
+    F = 1.0 + 0.3 * rng.normal(size=n) + 0.1j
+    for prec in (twmc.PREC_F32, twmc.PREC_F64):
+        res, refs = square_case(oracle, 32, 32, ntraj=3, prec=prec, omega=omega, U=U, F=F)
+        check(res, refs, prec)
+
+
+@pytest.mark.parametrize("prec", [twmc.PREC_F32, twmc.PREC_F64])
+@pytest.mark.parametrize("ncell,pbc", [(256, True), (24, False), (1, True), (7, True)])
+def test_lieb_parity(built_lib, oracle, ncell, pbc, prec):
+    rng = np.random.default_rng(ncell)
+    E = 0.1 * rng.normal(size=3 * ncell)
+    U = 0.27 + 0.06 * rng.random(size=3 * ncell)
+    res, refs = lieb_case(oracle, ncell, pbc=pbc, prec=prec, E=E, U=U, F=0.3, detuning=0.5)
+    assert res["kernel"] == "ell_kernel<table>"
+    check(res, refs, prec)
+
+
+@pytest.mark.parametrize("prec", [twmc.PREC_F32, twmc.PREC_F64])
+def test_lieb_time_dependent_drive(built_lib, oracle, prec):
+    """C4-style drive: B sites only, linear ramp tabulated every 0.01, then held."""
+    ncell = 256
+    n = 3 * ncell
+    times = np.round(np.arange(0, 0.25 + 1e-9, 0.01), 10)
+    vals = np.zeros((len(times), n), dtype=complex)
+    vals[:, 1::3] = (2.5 * times / 0.25)[:, None]
+    res, refs = lieb_case(oracle, ncell, prec=prec, steps=200, dt=0.002, F_t=(times, vals))
+    check(res, refs, prec)
