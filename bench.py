@@ -181,6 +181,8 @@ def main():
     ap.add_argument("--hop", default="fft", choices=["fft", "stencil"])
     ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--ntraj", type=int, default=NTRAJ, help="profiling cases only; the bench line uses 16384")
     args = ap.parse_args()
     rank, world, local = env_rank()
     if args.impl == "reference":
@@ -200,7 +202,8 @@ def main():
     build_ext.build()
     fp32_peak = twmc.measure_fp32_peak()
     sysd = make_system(twmc, twmc.HOP_STENCIL if args.hop == "stencil" else None)
-    tasks = sysd.make_tasks(NTRAJ, t_start=0.0, t_end=T_END, seed0=1000 + rank * NTRAJ, id0=1 + rank * NTRAJ)
+    ntraj = args.ntraj
+    tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=T_END, seed0=1000 + rank * ntraj, id0=1 + rank * ntraj)
     sysd.batch_init(tasks)
     for _ in range(max(args.warmup, 3)):
         sysd.advance(FRAME_STEPS)
@@ -237,7 +240,7 @@ def main():
     del field
     info_kernel = sysd.kernel_name
     sysd.close()
-    su_rank = float(args.steps) * FRAME_STEPS * NTRAJ * NX * NY
+    su_rank = float(args.steps) * FRAME_STEPS * ntraj * NX * NY
     t_max = elapsed_ms
     if dist:
         t = torch.tensor([elapsed_ms], dtype=torch.float64, device="cuda")
@@ -248,7 +251,7 @@ def main():
     achieved = su_rank * FLOPS_PER_SITE_UPDATE / (kernel_ms / 1e3) / 1e12
     # end to end through the C ABI with host buffers (twmc_run)
     e2e = None
-    if rank == 0 or world > 1:
+    if not args.no_e2e:
         sysd = make_system(twmc, twmc.HOP_STENCIL if args.hop == "stencil" else None)
         tasks = sysd.make_tasks(NTRAJ, t_start=0.0, t_end=args.e2e_steps * FRAME_STEPS * DT, seed0=7,
                                 store_initial=False)
@@ -274,7 +277,7 @@ def main():
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": t_max / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Philox disorder / noise)",
-        "config": dict(CONFIG, hop=args.hop, kernel=info_kernel),
+        "config": dict(CONFIG, hop=args.hop, kernel=info_kernel, trajectories=ntraj),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak if fp32_peak else None, "traffic": ncu_traffic(),
                      "peak_source": "measured in this run: FP32 FMA chain over all SMs (twmc_measure_fp32_peak)",
