@@ -277,34 +277,19 @@ void setup_params(twmc_handle* h) {
 int build_tables(twmc_handle* h) {
   const int prec = h->prec;
   if (h->use_fft) {
-    PlanView pv;
-    square_plan(h->bx, h->by, &pv);
     const int64_t M0 = int64_t(1) << h->by, M1 = int64_t(1) << h->bx;
     std::vector<cd> tw;
     for (int64_t j = 0; j < M0; ++j) tw.push_back(std::polar(1.0, -2.0 * M_PI * double(j) / double(M0)));
     for (int64_t j = 0; j < M1; ++j) tw.push_back(std::polar(1.0, -2.0 * M_PI * double(j) / double(M1)));
     if (!upload_c(&h->d_tw, tw, prec)) return fail(h, TWMC_ERR_NOMEM, "twiddle table upload");
-    // k-space table at the last pass's positions, [slot][thread] order.
-    const int E = 1 << pv.e;
-    const int64_t tpt = h->nsites / E;
+    // separable k-space table: [2J fy cos(2 pi ky / ny) / N for ky < M0 |
+    // 2J fx cos(2 pi kx / nx) / N for kx < M1]; the kernel adds the two.
     const double fx = (h->nx == 1) ? 0.0 : 1.0, fy = (h->ny == 1) ? 0.0 : 1.0;
-    std::vector<double> kt(size_t(h->nsites));
-    for (int s = 0; s < E; ++s) {
-      for (int64_t t = 0; t < tpt; ++t) {
-        int64_t p = 0;
-        for (int j = 0; j < pv.e; ++j) p |= int64_t((s >> j) & 1) << pv.reg_last[j];
-        for (int i = 0; i < pv.nthr; ++i) p |= int64_t((t >> i) & 1) << pv.thr_last[i];
-        const int64_t pc = p & (M0 - 1), pr = p >> h->by;
-        int64_t ky = 0, kx = 0;
-        for (int b = 0; b < h->by; ++b) ky |= ((pc >> b) & 1) << (h->by - 1 - b);
-        for (int b = 0; b < h->bx; ++b) kx |= ((pr >> b) & 1) << (h->bx - 1 - b);
-        const double v = 2.0 * h->J *
-                         (fx * std::cos(2.0 * M_PI / double(h->nx) * double(kx)) +
-                          fy * std::cos(2.0 * M_PI / double(h->ny) * double(ky))) /
-                         double(h->nsites);
-        kt[size_t(s * tpt + t)] = v;
-      }
-    }
+    std::vector<double> kt;
+    for (int64_t k = 0; k < M0; ++k)
+      kt.push_back(2.0 * h->J * fy * std::cos(2.0 * M_PI / double(h->ny) * double(k)) / double(h->nsites));
+    for (int64_t k = 0; k < M1; ++k)
+      kt.push_back(2.0 * h->J * fx * std::cos(2.0 * M_PI / double(h->nx) * double(k)) / double(h->nsites));
     if (!upload_r(&h->d_ktab, kt, prec)) return fail(h, TWMC_ERR_NOMEM, "k table upload");
   } else if (h->lattice == TWMC_LATTICE_LIEB) {
     // Coupling triplets of TWMCLiebSolver::Setup (TWMCLiebSolver.cpp:54-85).
@@ -408,6 +393,9 @@ int advance(twmc_handle* h, int64_t n, bool want_nk) {
   if (any_traj) for (int k = 0; k < 3; ++k) if (h->par_shared[k]) *par[k] = h->d_par[k].p;
   a.dt = h->dt;
   a.dt4 = std::sqrt(h->gamma * h->dt / 4.0);
+  for (int k = 0; k < 3; ++k) { a.f_par[2 * k] = float(sc[k][0]); a.f_par[2 * k + 1] = float(sc[k][1]); }
+  a.f_dt = float(a.dt);
+  a.f_dt4 = float(a.dt4);
   a.noise_mode = h->noise_mode;
   a.noise = h->d_noise.p;
   a.noise_traj_stride = h->noise_steps * h->nsites;

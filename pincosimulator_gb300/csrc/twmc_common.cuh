@@ -66,7 +66,9 @@ __device__ __forceinline__ float2 normal_pair(uint32_t a, uint32_t b, float) {
   const float u1 = __fmaf_rn(__uint2float_rn(a), 0x1p-32f, 0x1p-33f);
   const float u2 = __fmaf_rn(__uint2float_rn(b), 0x1p-32f, 0x1p-33f);
   const float th = __fmaf_rn(u2, 6.28318530717958647692f, -3.14159265358979323846f);
-  const float r = sqrtf(fmaxf(-2.0f * logf(u1), 0.0f));
+  // r = sqrt(-2 ln u1) with the hardware log2 / reciprocal square root
+  const float r2 = fmaxf(-2.0f * __logf(u1), 0.0f);
+  const float r = r2 * rsqrtf(fmaxf(r2, 1e-30f));
   float s, c;
   __sincosf(th, &s, &c);
   return make_float2(r * c, r * s);

@@ -37,6 +37,8 @@ struct StepArgs {
   int64_t par_stride;     // elements between trajectories (0 = shared)
   double rsl_s[2], iU_s[2], iF_s[2];
   double dt, dt4;
+  float f_par[6];         // FP32 copies of rsl_s, iU_s, iF_s
+  float f_dt, f_dt4;
   // noise
   int noise_mode;         // 0 Philox, 1 buffer
   const void* noise;      // [ntraj][noise_steps][N] complex (R)
@@ -46,7 +48,7 @@ struct StepArgs {
   int* status;            // [ntraj]
   // square FFT kernel tables
   const void* tw;         // [M0 + M1] complex R: W_M^j per dimension
-  const void* ktab;       // [E][TPT] R: 2J(cos kx + cos ky)/N at last-pass positions
+  const void* ktab;       // [M0 + M1] R: 2J cos(2 pi k / n) / N per dimension (columns, then rows)
   // ell kernel
   int tpt;                // threads per trajectory
   int64_t nsites;         // N
@@ -97,6 +99,9 @@ template <class P> struct PlanInfo {
   static constexpr int TPT = N / E;
   static constexpr int M0 = 1 << P::m[0];
   static constexpr int M1 = 1 << P::m[1];
+  // twiddle entries read: exponents below 3M/4 (radix-4) and M/2 (radix-2)
+  static constexpr int TW0 = M0 >= 4 ? 3 * M0 / 4 : 1;
+  static constexpr int TW1 = M1 >= 4 ? 3 * M1 / 4 : 1;
   static constexpr int slot_bit(int k, int g) {
     for (int j = 0; j < P::e; ++j) if (P::reg[k][j] == g) return j;
     return -1;
@@ -111,6 +116,18 @@ template <class P> struct PlanInfo {
     for (int i = 0; i < P::nthr; ++i) m |= 1u << P::thr[k][i];
     return P::nthr ? m : 0u;
   }
+  static constexpr int bitrev(int v, int nb) {
+    int r = 0;
+    for (int i = 0; i < nb; ++i) r |= ((v >> i) & 1) << (nb - 1 - i);
+    return r;
+  }
+  // k-space indices of position p after the forward plan (bit reversal per dim)
+  static constexpr int ky_of(int p) { return bitrev(p & ((1 << P::by) - 1), P::by); }
+  static constexpr int kx_of(int p) { return P::bx ? bitrev(p >> P::by, P::bx) : 0; }
+  static constexpr bool last_has_row_reg() {
+    for (int j = 0; j < P::e; ++j) if (P::reg[P::npass - 1][j] >= P::by) return true;
+    return false;
+  }
   // slot index with zero bits inserted at positions j0 (and j1 if >= 0)
   static constexpr int insert0(int q, int j0, int j1) {
     int s = 0, src = 0;
@@ -123,12 +140,10 @@ template <class P> struct PlanInfo {
   }
 };
 
-// Swizzle of the CTA-flat element index (XOR of bits 4..7 into 0..3): linear
-// over XOR, so thread and register parts are swizzled separately.
-template <int FLAT_BITS>
-__host__ __device__ constexpr int swz(int p) {
-  return FLAT_BITS >= 8 ? (p ^ ((p >> 4) & 15)) : p;
-}
+// Padded position of the CTA-flat element index: one pad slot after every 16
+// elements. For indices with disjoint bits pad(a | b) = pad(a) + pad(b), so
+// the thread part is a register and the register-slot part an immediate.
+__host__ __device__ constexpr int pad16(int p) { return p + (p >> 4); }
 
 // One DIF stage (forward) or its adjoint (inverse) of pass K, stage SI.
 template <class P, int K, int SI, bool INV, typename T>
@@ -222,43 +237,43 @@ __device__ __forceinline__ void fft_pass(T (&x)[PlanInfo<P>::E], const T* tw0, c
 }
 
 // Exchange from layout of pass KA to layout of pass KB through shared memory.
-template <class P, int KA, int KB, int FLAT_BITS, bool SYNC_WARP, typename T>
+template <class P, int KA, int KB, bool SYNC_WARP, typename T>
 __device__ __forceinline__ void fft_exchange(T (&x)[PlanInfo<P>::E], T* __restrict__ buf, int base_a,
                                              int base_b) {
   using I = PlanInfo<P>;
   static_for<I::E>([&](auto S) {
     constexpr int s = decltype(S)::value;
-    constexpr int off = swz<FLAT_BITS>(I::pos_reg(KA, s));
-    buf[base_a ^ off] = x[s];
+    constexpr int off = pad16(I::pos_reg(KA, s));
+    buf[base_a + off] = x[s];
   });
   if constexpr (SYNC_WARP) __syncwarp(); else __syncthreads();
   static_for<I::E>([&](auto S) {
     constexpr int s = decltype(S)::value;
-    constexpr int off = swz<FLAT_BITS>(I::pos_reg(KB, s));
-    x[s] = buf[base_b ^ off];
+    constexpr int off = pad16(I::pos_reg(KB, s));
+    x[s] = buf[base_b + off];
   });
 }
 
-template <class P, int CTA>
+template <class P, int CTA, typename R>
 struct SquareCfg {
+  static constexpr bool BETA_SMEM = sizeof(R) == 4;
   using I = PlanInfo<P>;
   static constexpr int E = I::E, N = I::N, TPT = I::TPT;
   static constexpr int TPC = CTA / TPT;  // trajectories per CTA
-  static constexpr int FLAT_BITS = P::nbits + (TPC > 1 ? (TPC == 2 ? 1 : TPC == 4 ? 2 : TPC == 8 ? 3 : TPC == 16 ? 4 : TPC == 32 ? 5 : TPC == 64 ? 6 : 7) : 0);
+  static constexpr int XSZ = TPC * N + (TPC * N) / 16;  // one padded exchange buffer
   static constexpr bool SYNC_WARP = TPT <= 32;
-  template <typename R>
-  static constexpr size_t smem_bytes(int nparams) {
+  static constexpr size_t smem_bytes() {
     using T = c2_t<R>;
-    return sizeof(T) * (size_t(I::M0 + I::M1) + 2 * size_t(TPC) * N + size_t(nparams) * TPC * N) +
-           sizeof(R) * size_t(N);
+    return sizeof(T) * (size_t(I::TW0 + I::TW1) + 2 * size_t(XSZ) + (BETA_SMEM ? size_t(TPC) * N : 0)) +
+           sizeof(R) * size_t(I::M0 + I::M1);
   }
 };
 
 template <typename R, class P, int CTA>
-__global__ void __launch_bounds__(CTA) square_fft_kernel(const StepArgs a) {
+__global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel(const StepArgs a) {
   using T = c2_t<R>;
   using I = PlanInfo<P>;
-  using Cfg = SquareCfg<P, CTA>;
+  using Cfg = SquareCfg<P, CTA, R>;
   constexpr int E = I::E, N = I::N, TPT = I::TPT, TPC = Cfg::TPC;
   constexpr int NP = P::npass;
   constexpr int LAST = NP - 1;
@@ -267,25 +282,27 @@ __global__ void __launch_bounds__(CTA) square_fft_kernel(const StepArgs a) {
 
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s_tw = reinterpret_cast<T*>(smem_raw);
-  T* s_x = s_tw + (I::M0 + I::M1);         // 2 exchange buffers of TPC * N
-  T* s_par = s_x + 2 * TPC * N;             // per-site params, thread-private slices
+  T* s_x = s_tw + (I::TW0 + I::TW1);       // 2 padded exchange buffers of Cfg::XSZ
+  // FP32: the state lives in thread-private smem slices [slot][s][t] (frees
+  // 32 registers for a second CTA per SM); FP64: in registers.
+  constexpr bool BETA_SMEM = Cfg::BETA_SMEM;
+  T* s_beta = s_x + 2 * Cfg::XSZ;
+  // separable k-space table: s_k = ky table [M0] + kx table [M1] (2J cos / N)
+  R* s_kt = reinterpret_cast<R*>(s_beta + (BETA_SMEM ? TPC * N : 0));
   const bool has_rsl = a.rsl != nullptr, has_iU = a.iU != nullptr, has_iF = a.iF != nullptr;
-  // per-site parameters live in thread-private smem slices when they fit
-  // (a.dbuf = 1), else they are read from global memory every step
-  const bool par_smem = a.dbuf != 0;
-  const int nparams = par_smem ? int(has_rsl) + int(has_iU) + int(has_iF) : 0;
-  R* s_k = reinterpret_cast<R*>(s_par + nparams * TPC * N);
+  // per-site parameters (thread-private) are read through L1 every step
 
   const int tid = threadIdx.x;
   const int slot = tid / TPT;
   const int t = tid % TPT;
 
   // tables
-  for (int i = tid; i < I::M0 + I::M1; i += CTA) s_tw[i] = reinterpret_cast<const T*>(a.tw)[i];
-  for (int i = tid; i < N; i += CTA) s_k[i] = reinterpret_cast<const R*>(a.ktab)[i];
+  for (int i = tid; i < I::TW0; i += CTA) s_tw[i] = reinterpret_cast<const T*>(a.tw)[i];
+  for (int i = tid; i < I::TW1; i += CTA) s_tw[I::TW0 + i] = reinterpret_cast<const T*>(a.tw)[I::M0 + i];
+  for (int i = tid; i < I::M0 + I::M1; i += CTA) s_kt[i] = reinterpret_cast<const R*>(a.ktab)[i];
   __syncthreads();
   const T* tw0 = s_tw;
-  const T* tw1 = s_tw + I::M0;
+  const T* tw1 = s_tw + I::TW0;
 
   // thread part of each pass's positions, and exchange bases
   int pos_thr[NP];
@@ -299,16 +316,19 @@ __global__ void __launch_bounds__(CTA) square_fft_kernel(const StepArgs a) {
       p |= ((t >> i) & 1) << b;
     });
     pos_thr[k] = p;
-    xbase[k] = swz<Cfg::FLAT_BITS>((slot << P::nbits) | p);
+    xbase[k] = pad16((slot << P::nbits) | p);
   });
 
-  const R dt = R(a.dt), dt4 = R(a.dt4);
-  const T rsl_s = cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
-  const T iU_s = cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
-  const T iF_s = cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
-  T* par_rsl = s_par;
-  T* par_iU = par_rsl + (has_rsl ? TPC * N : 0);
-  T* par_iF = par_iU + (has_iU ? TPC * N : 0);
+  // thread parts of the k-space indices in the last pass's layout
+  const int ky_t = I::bitrev(pos_thr[LAST] & ((1 << P::by) - 1), P::by);
+  const int kx_t = P::bx ? I::bitrev(pos_thr[LAST] >> P::by, P::bx) : 0;
+  const R* s_ky = s_kt + ky_t;
+  const R* s_kx = s_kt + I::M0 + kx_t;
+  const R kx_const = s_kx[0];  // used when no register bit is a row bit
+  const R dt = sizeof(R) == 4 ? R(a.f_dt) : R(a.dt), dt4 = sizeof(R) == 4 ? R(a.f_dt4) : R(a.dt4);
+  const T rsl_s = sizeof(R) == 4 ? cmake<T>(R(a.f_par[0]), R(a.f_par[1])) : cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
+  const T iU_s = sizeof(R) == 4 ? cmake<T>(R(a.f_par[2]), R(a.f_par[3])) : cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
+  const T iF_s = sizeof(R) == 4 ? cmake<T>(R(a.f_par[4]), R(a.f_par[5])) : cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
 
   int buf = 0;
   const int64_t ngroups = (a.ntraj + TPC - 1) / TPC;
@@ -317,37 +337,34 @@ __global__ void __launch_bounds__(CTA) square_fft_kernel(const StepArgs a) {
     const bool active = traj < a.ntraj;
     const int64_t tr = active ? traj : 0;
     T* st = reinterpret_cast<T*>(a.state) + tr * N;
-    T beta[E];
+    T* my_beta = s_beta + slot * N + t;  // element s at my_beta[s * TPT]
+    T rbeta[BETA_SMEM ? 1 : E];
+    auto bget = [&](auto S) -> T {
+      constexpr int s = decltype(S)::value;
+      if constexpr (BETA_SMEM) return my_beta[s * TPT]; else return rbeta[s];
+    };
+    auto bset = [&](auto S, T v) {
+      constexpr int s = decltype(S)::value;
+      if constexpr (BETA_SMEM) my_beta[s * TPT] = v; else rbeta[s] = v;
+    };
     static_for<E>([&](auto S) {
       constexpr int s = decltype(S)::value;
-      beta[s] = st[pos_thr[0] | I::pos_reg(0, s)];
+      bset(S, st[pos_thr[0] | I::pos_reg(0, s)]);
     });
-    // per-site parameters of this trajectory -> thread-private smem slices
-    const T* g_rsl = has_rsl ? reinterpret_cast<const T*>(a.rsl) + tr * a.par_stride : nullptr;
-    const T* g_iU = has_iU ? reinterpret_cast<const T*>(a.iU) + tr * a.par_stride : nullptr;
-    const T* g_iF = has_iF ? reinterpret_cast<const T*>(a.iF) + tr * a.par_stride : nullptr;
-    if (par_smem) {
-      static_for<E>([&](auto S) {
-        constexpr int s = decltype(S)::value;
-        const int p = pos_thr[0] | I::pos_reg(0, s);
-        const int q = (slot * E + s) * TPT + t;
-        if (has_rsl) par_rsl[q] = g_rsl[p];
-        if (has_iU) par_iU[q] = g_iU[p];
-        if (has_iF) par_iF[q] = g_iF[p];
-      });
-    }
+    const T* __restrict__ g_rsl = has_rsl ? reinterpret_cast<const T*>(a.rsl) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iU = has_iU ? reinterpret_cast<const T*>(a.iU) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iF = has_iF ? reinterpret_cast<const T*>(a.iF) + tr * a.par_stride : nullptr;
     const uint32_t seed = a.seeds[tr], id = a.ids[tr];
     const T* noise_tr = reinterpret_cast<const T*>(a.noise) + tr * a.noise_traj_stride;
 
     for (int64_t step = 0; step < a.nsteps; ++step) {
       T x[E];
-#pragma unroll
-      for (int s = 0; s < E; ++s) x[s] = beta[s];
+      static_for<E>([&](auto S) { x[decltype(S)::value] = bget(S); });
       // forward FFT
       static_for<NP>([&](auto KK) {
         constexpr int k = decltype(KK)::value;
         if constexpr (k > 0) {
-          fft_exchange<P, k - 1, k, Cfg::FLAT_BITS, Cfg::SYNC_WARP>(x, s_x + buf * TPC * N, xbase[k - 1], xbase[k]);
+          fft_exchange<P, k - 1, k, Cfg::SYNC_WARP>(x, s_x + buf * Cfg::XSZ, xbase[k - 1], xbase[k]);
           buf ^= 1;
         }
         fft_pass<P, k, false>(x, tw0, tw1, pos_thr[k]);
@@ -355,7 +372,9 @@ __global__ void __launch_bounds__(CTA) square_fft_kernel(const StepArgs a) {
       // k-space multiply by -i 2J (cos kx + cos ky) / N
       static_for<E>([&](auto S) {
         constexpr int s = decltype(S)::value;
-        const R sk = s_k[s * TPT + t];
+        constexpr int pr = I::pos_reg(LAST, s);
+        R sk = s_ky[I::ky_of(pr)];
+        if constexpr (I::last_has_row_reg()) sk += s_kx[I::kx_of(pr)]; else sk += kx_const;
         x[s] = cmake<T>(sk * x[s].y, -sk * x[s].x);
       });
       // inverse FFT (adjoint passes in reverse order)
@@ -363,7 +382,7 @@ __global__ void __launch_bounds__(CTA) square_fft_kernel(const StepArgs a) {
         constexpr int k = LAST - decltype(KK)::value;
         fft_pass<P, k, true>(x, tw0, tw1, pos_thr[k]);
         if constexpr (k > 0) {
-          fft_exchange<P, k, k - 1, Cfg::FLAT_BITS, Cfg::SYNC_WARP>(x, s_x + buf * TPC * N, xbase[k], xbase[k - 1]);
+          fft_exchange<P, k, k - 1, Cfg::SYNC_WARP>(x, s_x + buf * Cfg::XSZ, xbase[k], xbase[k - 1]);
           buf ^= 1;
         }
       });
@@ -384,21 +403,17 @@ __global__ void __launch_bounds__(CTA) square_fft_kernel(const StepArgs a) {
           xi_hi = nz[pos_thr[0] | I::pos_reg(0, s_hi)];
         }
         T r_lo = rsl_s, r_hi = rsl_s, u_lo = iU_s, u_hi = iU_s, f_lo = iF_s, f_hi = iF_s;
-        if (par_smem) {
-          const int qlo = (slot * E + s_lo) * TPT + t;
-          const int qhi = (slot * E + s_hi) * TPT + t;
-          if (has_rsl) { r_lo = par_rsl[qlo]; r_hi = par_rsl[qhi]; }
-          if (has_iU) { u_lo = par_iU[qlo]; u_hi = par_iU[qhi]; }
-          if (has_iF) { f_lo = par_iF[qlo]; f_hi = par_iF[qhi]; }
-        } else {
+        {
           const int plo = pos_thr[0] | I::pos_reg(0, s_lo);
           const int phi = pos_thr[0] | I::pos_reg(0, s_hi);
           if (has_rsl) { r_lo = __ldg(g_rsl + plo); r_hi = __ldg(g_rsl + phi); }
           if (has_iU) { u_lo = __ldg(g_iU + plo); u_hi = __ldg(g_iU + phi); }
           if (has_iF) { f_lo = __ldg(g_iF + plo); f_hi = __ldg(g_iF + phi); }
         }
-        beta[s_lo] = local_update(beta[s_lo], x[s_lo], r_lo, u_lo, f_lo, dt, dt4, xi_lo);
-        beta[s_hi] = local_update(beta[s_hi], x[s_hi], r_hi, u_hi, f_hi, dt, dt4, xi_hi);
+        constexpr std::integral_constant<int, s_lo> SL{};
+        constexpr std::integral_constant<int, s_hi> SH{};
+        bset(SL, local_update(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, dt4, xi_lo));
+        bset(SH, local_update(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, dt4, xi_hi));
       });
     }
 
@@ -407,20 +422,20 @@ __global__ void __launch_bounds__(CTA) square_fft_kernel(const StepArgs a) {
     if (active) {
       static_for<E>([&](auto S) {
         constexpr int s = decltype(S)::value;
-        st[pos_thr[0] | I::pos_reg(0, s)] = beta[s];
-        bad |= !finite_c(beta[s]);
+        const T b = bget(S);
+        st[pos_thr[0] | I::pos_reg(0, s)] = b;
+        bad |= !finite_c(b);
       });
       set_status(a.status, traj, bad);
     }
     // |FFT(beta)|^2 / N of the final state for the k-space populations
     if (a.nk != nullptr) {
       T x[E];
-#pragma unroll
-      for (int s = 0; s < E; ++s) x[s] = beta[s];
+      static_for<E>([&](auto S) { x[decltype(S)::value] = bget(S); });
       static_for<NP>([&](auto KK) {
         constexpr int k = decltype(KK)::value;
         if constexpr (k > 0) {
-          fft_exchange<P, k - 1, k, Cfg::FLAT_BITS, Cfg::SYNC_WARP>(x, s_x + buf * TPC * N, xbase[k - 1], xbase[k]);
+          fft_exchange<P, k - 1, k, Cfg::SYNC_WARP>(x, s_x + buf * Cfg::XSZ, xbase[k - 1], xbase[k]);
           buf ^= 1;
         }
         fft_pass<P, k, false>(x, tw0, tw1, pos_thr[k]);
@@ -473,17 +488,13 @@ __global__ void __launch_bounds__(CTA) ell_kernel(const StepArgs a) {
     site[v] = valid[v] ? int(s) : 0;
   }
   uint32_t nb01[VPT], nb23[VPT];
-  T nw[HOP == 0 ? VPT : 1][4];
 #pragma unroll
   for (int v = 0; v < VPT; ++v) {
     const int p = site[v];
     int n4[4];
     if constexpr (HOP == 0) {
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
-        n4[j] = a.nbr_idx[int64_t(p) * 4 + j];
-        nw[v][j] = reinterpret_cast<const T*>(a.nbr_w)[int64_t(p) * 4 + j];
-      }
+      for (int j = 0; j < 4; ++j) n4[j] = a.nbr_idx[int64_t(p) * 4 + j];
     } else {
       const int64_t nx = a.nx, ny = a.ny;
       const int64_t r = p / ny, c = p % ny;
@@ -495,6 +506,7 @@ __global__ void __launch_bounds__(CTA) ell_kernel(const StepArgs a) {
     nb01[v] = uint32_t(n4[0]) | (uint32_t(n4[1]) << 16);
     nb23[v] = uint32_t(n4[2]) | (uint32_t(n4[3]) << 16);
   }
+  const T* __restrict__ g_w = reinterpret_cast<const T*>(a.nbr_w);
   const R wy = a.ny > 1 ? R(1) : R(0), wx = a.nx > 1 ? R(1) : R(0);
   const R J = R(a.J);
   const R dt = R(a.dt), dt4 = R(a.dt4);
@@ -511,15 +523,12 @@ __global__ void __launch_bounds__(CTA) ell_kernel(const StepArgs a) {
     const bool active = in_slot && traj < a.ntraj;
     const int64_t tr = active ? traj : 0;
     T* st = reinterpret_cast<T*>(a.state) + tr * N;
-    T beta[VPT], rsl[VPT], iU[VPT], iF[VPT];
+    const T* __restrict__ g_rsl = a.rsl ? reinterpret_cast<const T*>(a.rsl) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iU = a.iU ? reinterpret_cast<const T*>(a.iU) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iF = a.iF ? reinterpret_cast<const T*>(a.iF) + tr * a.par_stride : nullptr;
+    T beta[VPT];
 #pragma unroll
-    for (int v = 0; v < VPT; ++v) {
-      const int p = site[v];
-      beta[v] = active && valid[v] ? st[p] : cmake<T>(R(0), R(0));
-      rsl[v] = a.rsl ? reinterpret_cast<const T*>(a.rsl)[tr * a.par_stride + p] : rsl_s;
-      iU[v] = a.iU ? reinterpret_cast<const T*>(a.iU)[tr * a.par_stride + p] : iU_s;
-      iF[v] = a.iF ? reinterpret_cast<const T*>(a.iF)[tr * a.par_stride + p] : iF_s;
-    }
+    for (int v = 0; v < VPT; ++v) beta[v] = active && valid[v] ? st[site[v]] : cmake<T>(R(0), R(0));
     const uint32_t seed = a.seeds[tr], id = a.ids[tr];
     const T* noise_tr = reinterpret_cast<const T*>(a.noise) + tr * a.noise_traj_stride;
     for (int64_t step = 0; step < a.nsteps; ++step) {
@@ -528,34 +537,28 @@ __global__ void __launch_bounds__(CTA) ell_kernel(const StepArgs a) {
 #pragma unroll
       for (int v = 0; v < VPT; ++v) if (valid[v]) sb[site[v]] = beta[v];
       __syncthreads();
-      T h[VPT];
-#pragma unroll
-      for (int v = 0; v < VPT; ++v) {
+      // hopping term of slot v, read lazily from this step's buffer (the next
+      // step writes the other buffer, or waits at the second barrier)
+      auto hop = [&](int v) -> T {
         const T b0 = sb[nb01[v] & 0xFFFFu], b1 = sb[nb01[v] >> 16];
         const T b2 = sb[nb23[v] & 0xFFFFu], b3 = sb[nb23[v] >> 16];
         if constexpr (HOP == 0) {
-          T acc = cmul(nw[v][0], b0);
-          acc = cadd(acc, cmul(nw[v][1], b1));
-          acc = cadd(acc, cmul(nw[v][2], b2));
-          acc = cadd(acc, cmul(nw[v][3], b3));
-          h[v] = acc;
+          const T* w = g_w + int64_t(site[v]) * 4;
+          T acc = cmul(__ldg(w), b0);
+          acc = cadd(acc, cmul(__ldg(w + 1), b1));
+          acc = cadd(acc, cmul(__ldg(w + 2), b2));
+          return cadd(acc, cmul(__ldg(w + 3), b3));
         } else {
           const T sy = cadd(b0, b1), sx = cadd(b2, b3);
           const T s = cmake<T>(wy * sy.x + wx * sx.x, wy * sy.y + wx * sx.y);
-          h[v] = cmake<T>(J * s.y, -J * s.x);  // -i J s
+          return cmake<T>(J * s.y, -J * s.x);  // -i J s
         }
-      }
-      if (a.dbuf) buf ^= 1; else __syncthreads();
+      };
+      int id_t = 0;
+      R dtt = R(0);
       if (timedep) {
-        const int id_t = a.ft_id[gstep];
-        const R dtt = R(a.ft_dt[gstep]);
-        const T* fv = reinterpret_cast<const T*>(a.ft_vals) + int64_t(id_t) * N;
-        const T* fs = reinterpret_cast<const T*>(a.ft_slopes) + int64_t(id_t) * N;
-#pragma unroll
-        for (int v = 0; v < VPT; ++v) {
-          const T f0 = fv[site[v]], f1 = fs[site[v]];
-          iF[v] = cmake<T>(f0.x + dtt * f1.x, f0.y + dtt * f1.y);
-        }
+        id_t = a.ft_id[gstep];
+        dtt = R(a.ft_dt[gstep]);
       }
 #pragma unroll
       for (int v = 0; v < H; ++v) {
@@ -569,9 +572,22 @@ __global__ void __launch_bounds__(CTA) ell_kernel(const StepArgs a) {
           xi_lo = nz[site[v]];
           xi_hi = valid[v + H] ? nz[site[v + H]] : cmake<T>(R(0), R(0));
         }
-        beta[v] = local_update(beta[v], h[v], rsl[v], iU[v], iF[v], dt, dt4, xi_lo);
-        beta[v + H] = local_update(beta[v + H], h[v + H], rsl[v + H], iU[v + H], iF[v + H], dt, dt4, xi_hi);
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int vv = q ? v + H : v;
+          const int p = site[vv];
+          const T r = g_rsl ? __ldg(g_rsl + p) : rsl_s;
+          const T u = g_iU ? __ldg(g_iU + p) : iU_s;
+          T f = g_iF ? __ldg(g_iF + p) : iF_s;
+          if (timedep) {
+            const T f0 = __ldg(reinterpret_cast<const T*>(a.ft_vals) + int64_t(id_t) * N + p);
+            const T f1 = __ldg(reinterpret_cast<const T*>(a.ft_slopes) + int64_t(id_t) * N + p);
+            f = cmake<T>(f0.x + dtt * f1.x, f0.y + dtt * f1.y);
+          }
+          beta[vv] = local_update(beta[vv], hop(vv), r, u, f, dt, dt4, q ? xi_hi : xi_lo);
+        }
       }
+      if (a.dbuf) buf ^= 1; else __syncthreads();
     }
     if (active) {
       bool bad = false;

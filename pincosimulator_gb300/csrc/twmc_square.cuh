@@ -11,13 +11,13 @@
 
 namespace twmc {
 
-// Threads per CTA: whole trajectories, up to 256 threads, with the exchange
-// buffers and up to three per-site parameter slices of all trajectories of
-// the CTA inside a ~100 KB shared-memory budget.
+// Threads per CTA: whole trajectories, up to 256 threads, with the two
+// exchange buffers and the state slices of all trajectories of the CTA inside
+// a ~100 KB shared-memory budget.
 template <typename R, class P>
 constexpr int cta_for() {
   constexpr int tpt = PlanInfo<P>::TPT;
-  constexpr size_t per_traj = 5 * sizeof(c2_t<R>) * size_t(PlanInfo<P>::N);
+  constexpr size_t per_traj = (sizeof(R) == 4 ? 3 : 2) * sizeof(c2_t<R>) * size_t(PlanInfo<P>::N) * 17 / 16;
   int tpc = tpt >= 256 ? 1 : 256 / tpt;
   while (tpc > 1 && size_t(tpc) * per_traj > 100 * 1024) tpc /= 2;
   return tpc * tpt;
@@ -26,20 +26,22 @@ constexpr int cta_for() {
 template <typename R, class P>
 bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo* info, std::string* err) {
   constexpr int CTA = cta_for<R, P>();
-  using Cfg = SquareCfg<P, CTA>;
+  using Cfg = SquareCfg<P, CTA, R>;
+  (void)nparams;
+  const StepArgs a2 = a;
+  const size_t smem = Cfg::smem_bytes();
   int dev0 = 0, maxsm = 0;
   cudaGetDevice(&dev0);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev0);
-  StepArgs a2 = a;
-  size_t smem = Cfg::template smem_bytes<R>(nparams);
-  a2.dbuf = 1;  // parameters in shared memory
-  if (nparams > 0 && smem > size_t(maxsm) / 2) {
-    smem = Cfg::template smem_bytes<R>(0);
-    a2.dbuf = 0;  // parameters read from global memory
+  if (smem > size_t(maxsm)) {
+    if (err) *err = "square kernel needs " + std::to_string(smem) + " B of shared memory (device max " +
+                    std::to_string(maxsm) + ")";
+    return false;
   }
   auto fn = square_fft_kernel<R, P, CTA>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) {
+    cudaGetLastError();
     if (err) *err = std::string("square kernel smem attribute: ") + cudaGetErrorString(e);
     return false;
   }
@@ -48,6 +50,7 @@ bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo*
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, CTA, smem);
   if (e != cudaSuccess || per_sm <= 0) {
+    cudaGetLastError();
     if (err) *err = std::string("square kernel does not fit on an SM (smem ") + std::to_string(smem) + " B)";
     return false;
   }
