@@ -60,7 +60,49 @@ def _compile(src: str, verbose: bool) -> str:
     return obj
 
 
+HOST = os.path.join(HERE, "host")
+HOST_LIB = os.path.join(BUILD, "libtwmc_host.so")
+SIM = os.path.join(BUILD, "twmc_sim")
+HOST_SOURCES = ["Settings.cpp", "NoisyMatrix.cpp", "TWMC.cpp", "PincoFormat.cpp"]
+CXX = os.environ.get("CXX", "g++")
+
+
+def _host_hash() -> str:
+    h = hashlib.sha256()
+    for name in sorted(os.listdir(HOST)):
+        with open(os.path.join(HOST, name), "rb") as f:
+            h.update(name.encode() + f.read())
+    with open(os.path.join(HERE, "..", "include", "twmc.h"), "rb") as f:
+        h.update(f.read())
+    return h.hexdigest()
+
+
+def build_host(force: bool = False) -> str:
+    """libtwmc_host.so (Solver plugin layer, settings, archive) and twmc_sim."""
+    stamp = os.path.join(BUILD, "host_stamp.txt")
+    digest = _host_hash()
+    if not force and os.path.exists(SIM) and os.path.exists(stamp) and open(stamp).read() == digest:
+        return SIM
+    flags = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-Wno-sign-compare"]
+    link = ["-L" + BUILD, "-Wl,-rpath,$ORIGIN"]
+    srcs = [os.path.join(HOST, s) for s in HOST_SOURCES]
+    subprocess.run([CXX, *flags, "-shared", *srcs, "-o", HOST_LIB + ".tmp", *link, "-ltwmc_cuda"], check=True)
+    os.replace(HOST_LIB + ".tmp", HOST_LIB)
+    subprocess.run([CXX, *flags, os.path.join(HOST, "twmc_sim.cpp"), "-o", SIM + ".tmp", *link,
+                    "-Wl,--no-as-needed", "-ltwmc_host", "-ltwmc_cuda"], check=True)
+    os.replace(SIM + ".tmp", SIM)
+    with open(stamp, "w") as f:
+        f.write(digest)
+    return SIM
+
+
 def build(force: bool = False, verbose: bool = False) -> str:
+    lib = build_cuda(force=force, verbose=verbose)
+    build_host(force=force)
+    return lib
+
+
+def build_cuda(force: bool = False, verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     _write_plans()
     stamp = os.path.join(BUILD, "stamp.txt")
@@ -74,6 +116,10 @@ def build(force: bool = False, verbose: bool = False) -> str:
     os.replace(tmp, LIB)
     with open(stamp, "w") as f:
         f.write(digest)
+    # the host library links against this one
+    hs = os.path.join(BUILD, "host_stamp.txt")
+    if os.path.exists(hs):
+        os.remove(hs)
     return LIB
 
 
