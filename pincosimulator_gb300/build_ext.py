@@ -20,7 +20,7 @@ LIB = os.path.join(BUILD, "libtwmc_cuda.so")
 NVCC = os.environ.get("NVCC", "/usr/local/cuda/bin/nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
-         "-Xcompiler", "-fvisibility=hidden", "-DNDEBUG"]
+         "-Xcompiler", "-fvisibility=hidden", "-DNDEBUG", "-I", os.path.join(HERE, "..", "include")]
 SOURCES = ["twmc_api.cu", "twmc_square_f32.cu", "twmc_square_f64.cu", "twmc_ell.cu", "twmc_misc.cu"]
 
 
@@ -83,7 +83,7 @@ def build_host(force: bool = False) -> str:
     digest = _host_hash()
     if not force and os.path.exists(SIM) and os.path.exists(stamp) and open(stamp).read() == digest:
         return SIM
-    flags = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-Wno-sign-compare"]
+    flags = ["-std=c++17", "-O2", "-fPIC", "-Wall", "-Wno-sign-compare", "-I" + os.path.join(HERE, "..", "include")]
     link = ["-L" + BUILD, "-Wl,-rpath,$ORIGIN"]
     srcs = [os.path.join(HOST, s) for s in HOST_SOURCES]
     subprocess.run([CXX, *flags, "-shared", *srcs, "-o", HOST_LIB + ".tmp", *link, "-ltwmc_cuda"], check=True)

@@ -14,7 +14,7 @@
 #include <tuple>
 #include <vector>
 
-#include "../../include/twmc.h"
+#include "twmc.h"
 #include "fft_plans.inc"
 #include "twmc_kernels.cuh"
 #include "twmc_launch.h"
@@ -284,12 +284,12 @@ int build_tables(twmc_handle* h) {
     if (!upload_c(&h->d_tw, tw, prec)) return fail(h, TWMC_ERR_NOMEM, "twiddle table upload");
     // separable k-space table: [2J fy cos(2 pi ky / ny) / N for ky < M0 |
     // 2J fx cos(2 pi kx / nx) / N for kx < M1]; the kernel adds the two.
+    // the FP32 kernel folds dt into the hopping term (local_update_fused)
     const double fx = (h->nx == 1) ? 0.0 : 1.0, fy = (h->ny == 1) ? 0.0 : 1.0;
+    const double scale = 2.0 * h->J / double(h->nsites) * (prec == TWMC_PREC_F32 ? h->dt : 1.0);
     std::vector<double> kt;
-    for (int64_t k = 0; k < M0; ++k)
-      kt.push_back(2.0 * h->J * fy * std::cos(2.0 * M_PI / double(h->ny) * double(k)) / double(h->nsites));
-    for (int64_t k = 0; k < M1; ++k)
-      kt.push_back(2.0 * h->J * fx * std::cos(2.0 * M_PI / double(h->nx) * double(k)) / double(h->nsites));
+    for (int64_t k = 0; k < M0; ++k) kt.push_back(scale * fy * std::cos(2.0 * M_PI / double(h->ny) * double(k)));
+    for (int64_t k = 0; k < M1; ++k) kt.push_back(scale * fx * std::cos(2.0 * M_PI / double(h->nx) * double(k)));
     if (!upload_r(&h->d_ktab, kt, prec)) return fail(h, TWMC_ERR_NOMEM, "k table upload");
   } else if (h->lattice == TWMC_LATTICE_LIEB) {
     // Coupling triplets of TWMCLiebSolver::Setup (TWMCLiebSolver.cpp:54-85).

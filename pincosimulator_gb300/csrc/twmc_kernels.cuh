@@ -90,6 +90,20 @@ __device__ __forceinline__ T local_update(T b, T h, T rsl, T iU, T iF, R dt, R d
   return cmake<T>(nb.x + dt4 * xi.x, nb.y + dt4 * xi.y);
 }
 
+// FP32 form of the same update with dt folded in: b' = (A + B |b|^2) b + h' +
+// F' + dt4 xi, A = 1 + dt (rsl - iU), B = dt iU, F' = dt iF, h' = dt h (the
+// k-space table carries dt). Equal to local_update up to FP32 rounding.
+template <typename T, typename R>
+__device__ __forceinline__ T local_update_fused(T b, T hdt, T rsl, T iU, T iF, R dt, R dt4, T xi) {
+  const T A = cmake<T>(R(1) + dt * (rsl.x - iU.x), dt * (rsl.y - iU.y));
+  const T B = cmake<T>(dt * iU.x, dt * iU.y);
+  const R ab2 = b.x * b.x + b.y * b.y;
+  const T c = cmake<T>(A.x + B.x * ab2, A.y + B.y * ab2);
+  T nb = cmul(c, b);
+  nb = cmake<T>(nb.x + hdt.x + dt * iF.x, nb.y + hdt.y + dt * iF.y);
+  return cmake<T>(nb.x + dt4 * xi.x, nb.y + dt4 * xi.y);
+}
+
 // ------------------------------------------------------------------------
 // compile-time plan helpers (P = generated Plan_bx_by)
 // ------------------------------------------------------------------------
@@ -293,8 +307,10 @@ __global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel
   // per-site parameters (thread-private) are read through L1 every step
 
   const int tid = threadIdx.x;
-  const int slot = tid / TPT;
-  const int t = tid % TPT;
+  // one trajectory per CTA: the trajectory index (and its Philox key) is
+  // uniform across the CTA
+  const int slot = TPC == 1 ? 0 : tid / TPT;
+  const int t = TPC == 1 ? tid : tid % TPT;
 
   // tables
   for (int i = tid; i < I::TW0; i += CTA) s_tw[i] = reinterpret_cast<const T*>(a.tw)[i];
@@ -412,8 +428,13 @@ __global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel
         }
         constexpr std::integral_constant<int, s_lo> SL{};
         constexpr std::integral_constant<int, s_hi> SH{};
-        bset(SL, local_update(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, dt4, xi_lo));
-        bset(SH, local_update(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, dt4, xi_hi));
+        if constexpr (sizeof(R) == 4) {  // dt is folded into the k-space table
+          bset(SL, local_update_fused(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, dt4, xi_lo));
+          bset(SH, local_update_fused(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, dt4, xi_hi));
+        } else {
+          bset(SL, local_update(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, dt4, xi_lo));
+          bset(SH, local_update(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, dt4, xi_hi));
+        }
       });
     }
 

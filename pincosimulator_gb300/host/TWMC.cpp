@@ -7,7 +7,7 @@
 #include <iostream>
 #include <limits>
 
-#include "../../include/twmc.h"
+#include "twmc.h"
 
 namespace pinco {
 
