@@ -1,0 +1,83 @@
+"""Ensemble observables from the engine's FP64 moment blocks.
+
+The reference saves raw fields only (its analysis tools are not part of the
+project); these are the standard truncated-Wigner estimators. For Wigner
+samples a of the field: <a^+ a> = <|a|^2>_W - 1/2,
+<a^+2 a^2> = <|a|^4>_W - 2 <|a|^2>_W + 1/2, g2 = <a^+2 a^2> / <a^+ a>^2,
+n_k = <|a_k|^2>_W - 1/2 with the unitary FFT a_k = FFT(a) / sqrt(N).
+
+Moment blocks come from twmc_run / twmc_batch_reduce: block b holds FP64 sums
+over trajectories [b T / B, (b + 1) T / B) of |a|^2, |a|^4 and |a_k|^2.
+Standard errors use the batch means of the B blocks; g2 uses a
+delete-one-block jackknife.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+
+def block_sizes(ntraj: int, nblocks: int) -> np.ndarray:
+    b = np.arange(nblocks + 1)
+    edges = (b * ntraj) // nblocks
+    return np.diff(edges)
+
+
+def observables(moments: np.ndarray, ntraj: int) -> dict:
+    """moments: (..., B, N, 3) FP64 block sums -> dict of (..., N) arrays."""
+    m = np.asarray(moments, dtype=np.float64)
+    B = m.shape[-3]
+    cnt = block_sizes(ntraj, B).astype(np.float64)
+    used = cnt > 0
+    m = m[..., used, :, :]
+    cnt = cnt[used]
+    B = len(cnt)
+    shape = (1,) * (m.ndim - 3) + (B, 1)
+    c = cnt.reshape(shape)
+    tot = m.sum(axis=-3)
+    m2, m4, mk = tot[..., 0] / ntraj, tot[..., 1] / ntraj, tot[..., 2] / ntraj
+    n = m2 - 0.5
+    a2a2 = m4 - 2.0 * m2 + 0.5
+    with np.errstate(divide="ignore", invalid="ignore"):
+        g2 = a2a2 / n**2
+    nk = mk - 0.5
+    # batch means
+    bm2 = m[..., 0] / c
+    bm4 = m[..., 1] / c
+    bmk = m[..., 2] / c
+    def se(x):
+        if B < 2:
+            return np.full(x.shape[:-2] + x.shape[-1:], np.nan)
+        return x.std(axis=-2, ddof=1) / np.sqrt(B)
+    n_se = se(bm2)
+    nk_se = se(bmk)
+    # jackknife over blocks for g2
+    g2_se = np.full_like(n, np.nan)
+    if B >= 2:
+        s2, s4 = m[..., 0].sum(axis=-2), m[..., 1].sum(axis=-2)
+        jk = []
+        for b in range(B):
+            t = ntraj - cnt[b]
+            j2 = (s2 - m[..., b, :, 0]) / t
+            j4 = (s4 - m[..., b, :, 1]) / t
+            with np.errstate(divide="ignore", invalid="ignore"):
+                jk.append((j4 - 2 * j2 + 0.5) / (j2 - 0.5) ** 2)
+        jk = np.stack(jk, axis=-2)
+        g2_se = np.sqrt((B - 1) / B * ((jk - jk.mean(axis=-2, keepdims=True)) ** 2).sum(axis=-2))
+    return {"n": n, "n_se": n_se, "a2a2": a2a2, "g2": g2, "g2_se": g2_se, "nk": nk, "nk_se": nk_se,
+            "bm2": bm2}
+
+
+def time_to_steady_state(times: np.ndarray, nbar: np.ndarray, nbar_se: np.ndarray, tail: float = 0.25):
+    """Earliest save time after which the spatially averaged n stays within
+    max(1 SE, 1e-3 n_inf) of n_inf, n_inf = mean of the last `tail` of the frames."""
+    times = np.asarray(times)
+    nbar = np.asarray(nbar)
+    k0 = int(np.floor((1.0 - tail) * len(nbar)))
+    n_inf = float(np.mean(nbar[k0:]))
+    tol = np.maximum(np.asarray(nbar_se), 1e-3 * abs(n_inf))
+    ok = np.abs(nbar - n_inf) <= tol
+    # last frame that violates the band; steady from the next one on
+    bad = np.nonzero(~ok)[0]
+    k = 0 if len(bad) == 0 else int(bad[-1]) + 1
+    k = min(k, len(times) - 1)
+    return float(times[k]), n_inf
