@@ -196,6 +196,32 @@ TWMC_API void* twmc_stream(const twmc_handle* h);
  * step kernels). */
 TWMC_API int twmc_measure_fp32_peak(double* tflops);
 
+/* ---- allocation-free entry point ------------------------------------------ */
+
+/* k-space populations and FP64 moment blocks of a caller-owned device batch,
+ * without allocating any device memory. It has no counterpart in the
+ * reference. It is for callers that cannot allocate device memory: a host
+ * application whose own pool already owns the device, or a latency-critical
+ * loop where cudaMalloc's implicit synchronisation is not acceptable. It
+ * computes what twmc_batch_reduce returns after a twmc_batch_advance:
+ *   moments[b][p] = sums over trajectories [b T/B, (b+1) T/B) of
+ *                   (|a_p|^2, |a_p|^4, |FFT(a)_p|^2 / N)
+ * state:    device pointer, n_traj x nx*ny complex64 (interleaved floats),
+ *           site order as everywhere in this ABI; nx, ny powers of two of a
+ *           compiled square-lattice plan (1 x 32..4096, 16x16, 32x32, 64x64)
+ * moments:  device pointer, n_blocks x nx*ny x 3 doubles (fully written)
+ * stream:   cudaStream_t to run on (NULL = default stream)
+ * Limit: n_traj * nx * ny <= 4194304 (the 16 MiB scratch array that every
+ * device loading the library holds until the process exits); larger sizes,
+ * unsupported shapes and null pointers return TWMC_ERR_INVALID.
+ * The first call on a device looks up the scratch array's device address
+ * (cudaGetSymbolAddress, with that device current); make that first call
+ * before any stream capture. All calls share the one scratch array: calls
+ * that overlap on the GPU (different streams, or host threads without
+ * ordering) race. The call allocates nothing and does not synchronise. */
+TWMC_API int twmc_kspace_moments_noalloc(const void* state, int64_t n_traj, int64_t nx, int64_t ny,
+                                         int32_t n_blocks, double* moments, void* stream);
+
 /* ---- self-check entry points -------------------------------------------- */
 
 /* Philox4x32-10 evaluated on the GPU for n counters (ctr: n x 4, key: 2 words),

@@ -29,7 +29,7 @@ EXPORTED = [
     "twmc_version", "twmc_create", "twmc_run", "twmc_set_noise_buffer", "twmc_progress", "twmc_last_error",
     "twmc_destroy", "twmc_batch_init", "twmc_batch_advance", "twmc_batch_reduce", "twmc_sync",
     "twmc_batch_download", "twmc_launch_count", "twmc_kernel_name", "twmc_stream", "twmc_measure_fp32_peak",
-    "twmc_debug_philox",
+    "twmc_kspace_moments_noalloc", "twmc_debug_philox",
 ]
 
 
@@ -97,6 +97,8 @@ def load(path: str = LIB_PATH):
     lib.twmc_stream.argtypes = [C.c_void_p]
     lib.twmc_stream.restype = C.c_void_p
     lib.twmc_measure_fp32_peak.argtypes = [C.POINTER(C.c_double)]
+    lib.twmc_kspace_moments_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
+                                                C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
 
