@@ -196,6 +196,49 @@ TWMC_API void* twmc_stream(const twmc_handle* h);
  * step kernels). */
 TWMC_API int twmc_measure_fp32_peak(double* tflops);
 
+/* ---- heterogeneous batch -------------------------------------------------- */
+
+/* One parameter point of a heterogeneous batch: a periodic square lattice
+ * (nx = 1 for a chain) with uniform complex parameters, n_traj trajectories
+ * with seeds seed0 + k and ids id0 + k, vacuum-style initial fields
+ * beta_init + beta_init_sigma * xi (TWMC_IC_SETTINGS), FP32 state. */
+typedef struct twmc_point_desc {
+  int64_t nx, ny;
+  double J, gamma, dt;
+  double omega[2], U[2], F[2];       /* complex values (re, im) */
+  double beta_init[2], beta_init_sigma[2];
+  int64_t n_traj;
+  uint32_t seed0;
+  uint64_t id0;
+  int32_t n_moment_blocks;           /* 0 = 32 (capped at n_traj) */
+} twmc_point_desc;
+
+typedef struct twmc_hbatch twmc_hbatch;
+
+/* Builds a batch of n points advanced together frame by frame: every point's
+ * trajectories of a shape with a register-FFT plan that fits 256 threads
+ * (chains of 32..1024 sites, 16x16, 32x32, 64x64 lattices) are served by one
+ * persistent launch with an atomic work queue; other shapes run the
+ * real-space kernel concurrently. One frame (frame_steps steps of every
+ * point, FP64 moment blocks, counters) is captured into a CUDA graph. tune:
+ * 1 = per shape, time the FFT path against the real-space path once and keep
+ * the faster (cached in $TWMC_TUNE_CACHE or ~/.cache/twmc_tune.json). */
+TWMC_API int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_steps, int32_t tune,
+                                twmc_hbatch** out);
+/* Replays the frame graph n_frames times (asynchronous). */
+TWMC_API int twmc_hbatch_run(twmc_hbatch* b, int64_t n_frames);
+/* Waits for the batch; *ms = device time of the last twmc_hbatch_run. */
+TWMC_API int twmc_hbatch_sync(twmc_hbatch* b, double* ms);
+/* Last frame's moment blocks of one point (n_blocks x sites x 3 doubles). */
+TWMC_API int twmc_hbatch_moments(twmc_hbatch* b, size_t point, double* out);
+/* Current field of one point (n_traj x sites complex128). */
+TWMC_API int twmc_hbatch_state(twmc_hbatch* b, size_t point, double* out);
+/* Kernel the point runs on. */
+TWMC_API const char* twmc_hbatch_plan(const twmc_hbatch* b, size_t point);
+TWMC_API const char* twmc_hbatch_last_error(const twmc_hbatch* b);
+TWMC_API int64_t twmc_hbatch_launch_count(const twmc_hbatch* b);
+TWMC_API void twmc_hbatch_destroy(twmc_hbatch* b);
+
 /* ---- allocation-free entry point ------------------------------------------ */
 
 /* k-space populations and FP64 moment blocks of a caller-owned device batch,

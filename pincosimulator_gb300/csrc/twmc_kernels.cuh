@@ -283,72 +283,74 @@ struct SquareCfg {
   }
 };
 
+// One square-lattice trajectory group (TPC trajectories) for a.nsteps steps:
+// the body of square_fft_kernel, shared with the heterogeneous-batch kernel.
+// Shared memory: twiddles | 2 padded exchange buffers | state slices (FP32) |
+// separable k-space table.
 template <typename R, class P, int CTA>
-__global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel(const StepArgs a) {
+struct SquareGroup {
   using T = c2_t<R>;
   using I = PlanInfo<P>;
   using Cfg = SquareCfg<P, CTA, R>;
-  constexpr int E = I::E, N = I::N, TPT = I::TPT, TPC = Cfg::TPC;
-  constexpr int NP = P::npass;
-  constexpr int LAST = NP - 1;
+  static constexpr int E = I::E, N = I::N, TPT = I::TPT, TPC = Cfg::TPC;
+  static constexpr int NP = P::npass;
+  static constexpr int LAST = NP - 1;
+  static constexpr bool BETA_SMEM = Cfg::BETA_SMEM;
   static_assert(CTA % TPT == 0, "CTA must hold whole trajectories");
   static_assert(P::reg[0][P::e - 1] == P::nbits - 1, "top bit must be a register bit of the first pass");
 
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  T* s_tw = reinterpret_cast<T*>(smem_raw);
-  T* s_x = s_tw + (I::TW0 + I::TW1);       // 2 padded exchange buffers of Cfg::XSZ
-  // FP32: the state lives in thread-private smem slices [slot][s][t] (frees
-  // 32 registers for a second CTA per SM); FP64: in registers.
-  constexpr bool BETA_SMEM = Cfg::BETA_SMEM;
-  T* s_beta = s_x + 2 * Cfg::XSZ;
-  // separable k-space table: s_k = ky table [M0] + kx table [M1] (2J cos / N)
-  R* s_kt = reinterpret_cast<R*>(s_beta + (BETA_SMEM ? TPC * N : 0));
-  const bool has_rsl = a.rsl != nullptr, has_iU = a.iU != nullptr, has_iF = a.iF != nullptr;
-  // per-site parameters (thread-private) are read through L1 every step
-
-  const int tid = threadIdx.x;
-  // one trajectory per CTA: the trajectory index (and its Philox key) is
-  // uniform across the CTA
-  const int slot = TPC == 1 ? 0 : tid / TPT;
-  const int t = TPC == 1 ? tid : tid % TPT;
-
-  // tables
-  for (int i = tid; i < I::TW0; i += CTA) s_tw[i] = reinterpret_cast<const T*>(a.tw)[i];
-  for (int i = tid; i < I::TW1; i += CTA) s_tw[I::TW0 + i] = reinterpret_cast<const T*>(a.tw)[I::M0 + i];
-  for (int i = tid; i < I::M0 + I::M1; i += CTA) s_kt[i] = reinterpret_cast<const R*>(a.ktab)[i];
-  __syncthreads();
-  const T* tw0 = s_tw;
-  const T* tw1 = s_tw + I::TW0;
-
-  // thread part of each pass's positions, and exchange bases
+  T* s_tw;
+  T* s_x;
+  T* s_beta;
+  R* s_kt;
+  int tid, slot, t;
   int pos_thr[NP];
   int xbase[NP];
-  static_for<NP>([&](auto KK) {
-    constexpr int k = decltype(KK)::value;
-    int p = 0;
-    static_for<P::nthr>([&](auto II) {
-      constexpr int i = decltype(II)::value;
-      constexpr int b = P::thr[k][i];
-      p |= ((t >> i) & 1) << b;
+
+  __device__ __forceinline__ explicit SquareGroup(unsigned char* smem_raw) {
+    s_tw = reinterpret_cast<T*>(smem_raw);
+    s_x = s_tw + (I::TW0 + I::TW1);
+    s_beta = s_x + 2 * Cfg::XSZ;
+    s_kt = reinterpret_cast<R*>(s_beta + (BETA_SMEM ? TPC * N : 0));
+    tid = threadIdx.x;
+    // one trajectory per CTA: the trajectory index (and its Philox key) is
+    // uniform across the CTA
+    slot = TPC == 1 ? 0 : tid / TPT;
+    t = TPC == 1 ? tid : tid % TPT;
+    static_for<NP>([&](auto KK) {
+      constexpr int k = decltype(KK)::value;
+      int p = 0;
+      static_for<P::nthr>([&](auto II) {
+        constexpr int i = decltype(II)::value;
+        constexpr int b = P::thr[k][i];
+        p |= ((t >> i) & 1) << b;
+      });
+      pos_thr[k] = p;
+      xbase[k] = pad16((slot << P::nbits) | p);
     });
-    pos_thr[k] = p;
-    xbase[k] = pad16((slot << P::nbits) | p);
-  });
+  }
 
-  // thread parts of the k-space indices in the last pass's layout
-  const int ky_t = I::bitrev(pos_thr[LAST] & ((1 << P::by) - 1), P::by);
-  const int kx_t = P::bx ? I::bitrev(pos_thr[LAST] >> P::by, P::bx) : 0;
-  const R* s_ky = s_kt + ky_t;
-  const R* s_kx = s_kt + I::M0 + kx_t;
-  const R kx_const = s_kx[0];  // used when no register bit is a row bit
-  const R dt = sizeof(R) == 4 ? R(a.f_dt) : R(a.dt), dt4 = sizeof(R) == 4 ? R(a.f_dt4) : R(a.dt4);
-  const T rsl_s = sizeof(R) == 4 ? cmake<T>(R(a.f_par[0]), R(a.f_par[1])) : cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
-  const T iU_s = sizeof(R) == 4 ? cmake<T>(R(a.f_par[2]), R(a.f_par[3])) : cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
-  const T iF_s = sizeof(R) == 4 ? cmake<T>(R(a.f_par[4]), R(a.f_par[5])) : cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
+  // twiddles and k-space table into shared memory (the caller synchronises)
+  __device__ __forceinline__ void load_tables(const StepArgs& a) {
+    for (int i = tid; i < I::TW0; i += CTA) s_tw[i] = reinterpret_cast<const T*>(a.tw)[i];
+    for (int i = tid; i < I::TW1; i += CTA) s_tw[I::TW0 + i] = reinterpret_cast<const T*>(a.tw)[I::M0 + i];
+    for (int i = tid; i < I::M0 + I::M1; i += CTA) s_kt[i] = reinterpret_cast<const R*>(a.ktab)[i];
+  }
 
-  int buf = 0;
-  const int64_t ngroups = (a.ntraj + TPC - 1) / TPC;
-  for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+  __device__ __forceinline__ void run(const StepArgs& a, int64_t g, int& buf) {
+    const T* tw0 = s_tw;
+    const T* tw1 = s_tw + I::TW0;
+    const bool has_rsl = a.rsl != nullptr, has_iU = a.iU != nullptr, has_iF = a.iF != nullptr;
+    // thread parts of the k-space indices in the last pass's layout
+    const int ky_t = I::bitrev(pos_thr[LAST] & ((1 << P::by) - 1), P::by);
+    const int kx_t = P::bx ? I::bitrev(pos_thr[LAST] >> P::by, P::bx) : 0;
+    const R* s_ky = s_kt + ky_t;
+    const R* s_kx = s_kt + I::M0 + kx_t;
+    const R kx_const = s_kx[0];  // used when no register bit is a row bit
+    const R dt = sizeof(R) == 4 ? R(a.f_dt) : R(a.dt), dt4 = sizeof(R) == 4 ? R(a.f_dt4) : R(a.dt4);
+    const T rsl_s = sizeof(R) == 4 ? cmake<T>(R(a.f_par[0]), R(a.f_par[1])) : cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
+    const T iU_s = sizeof(R) == 4 ? cmake<T>(R(a.f_par[2]), R(a.f_par[3])) : cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
+    const T iF_s = sizeof(R) == 4 ? cmake<T>(R(a.f_par[4]), R(a.f_par[5])) : cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
     const int64_t traj = g * TPC + slot;
     const bool active = traj < a.ntraj;
     const int64_t tr = active ? traj : 0;
@@ -474,6 +476,18 @@ __global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel
       }
     }
   }
+};
+
+template <typename R, class P, int CTA>
+__global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel(const StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  using G = SquareGroup<R, P, CTA>;
+  G grp(smem_raw);
+  grp.load_tables(a);
+  __syncthreads();
+  int buf = 0;
+  const int64_t ngroups = (a.ntraj + G::TPC - 1) / G::TPC;
+  for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x) grp.run(a, g, buf);
 }
 
 // ------------------------------------------------------------------------
@@ -486,10 +500,9 @@ __global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel
 // HOP = 1: square stencil h = -i J (wy (b[c+1] + b[c-1]) + wx (b[r+1] + b[r-1])).
 // ------------------------------------------------------------------------
 template <typename R, int VPT, int CTA, int HOP>
-__global__ void __launch_bounds__(CTA) ell_kernel(const StepArgs a) {
+__device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_raw) {
   using T = c2_t<R>;
   constexpr int H = VPT / 2;
-  extern __shared__ __align__(16) unsigned char smem_raw[];
   T* s_b = reinterpret_cast<T*>(smem_raw);
   const int64_t N = a.nsites;
   const int64_t half = (N + 1) / 2;
@@ -617,6 +630,24 @@ __global__ void __launch_bounds__(CTA) ell_kernel(const StepArgs a) {
       set_status(a.status, traj, bad);
     }
   }
+}
+
+template <typename R, int VPT, int CTA, int HOP>
+__global__ void __launch_bounds__(CTA) ell_kernel(const StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ell_body<R, VPT, CTA, HOP>(a, smem_raw);
+}
+
+// Same, with the arguments in device memory (kept there across the frames of a
+// captured graph); they are copied to shared memory first.
+template <typename R, int VPT, int CTA, int HOP>
+__global__ void __launch_bounds__(CTA) ell_kernel_dev(const StepArgs* __restrict__ ap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) StepArgs s_a;
+  for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += CTA)
+    reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(ap)[i];
+  __syncthreads();
+  ell_body<R, VPT, CTA, HOP>(s_a, smem_raw);
 }
 
 }  // namespace twmc

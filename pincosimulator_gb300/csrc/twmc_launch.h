@@ -49,11 +49,13 @@ struct InitArgs {
   const uint32_t* seeds;
   const uint32_t* ids;
   int ic_kind;              // per batch (twmc_ic_kind)
-  const double* binit;      // [N] complex
-  const double* bsigma;     // [N] complex
+  const double* binit;      // [N] complex, or NULL: binit_s
+  const double* bsigma;     // [N] complex, or NULL: bsigma_s
+  double binit_s[2], bsigma_s[2];
   const double* given;      // [ntraj][N] complex (ic_kind = GIVEN)
   // disorder: per matrix base [N], amp [N], kind; given realisations [ntraj][N] or NULL
-  const double* base[3];
+  const double* base[3];    // [N] complex, or NULL: base_s
+  double base_s[3][2];
   const double* amp[3];
   int kind[3];
   const double* given_real[3];

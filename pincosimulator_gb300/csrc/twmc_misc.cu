@@ -25,11 +25,11 @@ __global__ void init_kernel(const InitArgs a) {
     if (a.ic_kind == 2) {
       b = ld_c(a.given, i);
     } else {
-      b = a.binit ? ld_c(a.binit, p) : make_double2(0.0, 0.0);
+      b = a.binit ? ld_c(a.binit, p) : make_double2(a.binit_s[0], a.binit_s[1]);
       if (a.ic_kind == 0) {
         const u32x4 w = philox4x32_10(u32x4{c0, 0u, kStreamInit, 0u}, seed, id);
         const double2 z = hi ? normal_pair(w.z, w.w, 0.0) : normal_pair(w.x, w.y, 0.0);
-        const double2 sg = a.bsigma ? ld_c(a.bsigma, p) : make_double2(0.0, 0.0);
+        const double2 sg = a.bsigma ? ld_c(a.bsigma, p) : make_double2(a.bsigma_s[0], a.bsigma_s[1]);
         b = cadd(b, cmul(sg, z));
       }
     }
@@ -40,7 +40,7 @@ __global__ void init_kernel(const InitArgs a) {
         v[m] = ld_c(a.given_real[m], i);
         continue;
       }
-      v[m] = a.base[m] ? ld_c(a.base[m], p) : make_double2(0.0, 0.0);
+      v[m] = a.base[m] ? ld_c(a.base[m], p) : make_double2(a.base_s[m][0], a.base_s[m][1]);
       if (a.kind[m] != 0) {
         const u32x4 w = philox4x32_10(u32x4{c0, 0u, a.stream[m], 0u}, seed, id);
         const double2 amp = ld_c(a.amp[m], p);

@@ -22,11 +22,8 @@ struct KSum {
 // trajectory order: sum |a|^2, sum |a|^4, sum |a_k|^2. One thread per
 // (block, site); deterministic for a given (T, B).
 template <typename R>
-__global__ void moments_kernel(const MomentArgs a) {
+__device__ __forceinline__ void moments_site(const MomentArgs& a, int64_t p, int b) {
   using T = c2_t<R>;
-  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
-  const int b = blockIdx.y;
-  if (p >= a.nsites) return;
   const int64_t t0 = (int64_t(b) * a.ntraj) / a.nblocks, t1 = (int64_t(b + 1) * a.ntraj) / a.nblocks;
   // four interleaved partial sums (trajectory tr goes to partial tr % 4),
   // combined in fixed order: deterministic, four loads in flight per thread
@@ -68,6 +65,13 @@ __global__ void moments_kernel(const MomentArgs a) {
   o[0] = f2.value();
   o[1] = f4.value();
   o[2] = fk.value();
+}
+
+template <typename R>
+__global__ void moments_kernel(const MomentArgs a) {
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= a.nsites) return;
+  moments_site<R>(a, p, int(blockIdx.y));
 }
 
 }  // namespace twmc

@@ -30,6 +30,8 @@ EXPORTED = [
     "twmc_destroy", "twmc_batch_init", "twmc_batch_advance", "twmc_batch_reduce", "twmc_sync",
     "twmc_batch_download", "twmc_launch_count", "twmc_kernel_name", "twmc_stream", "twmc_measure_fp32_peak",
     "twmc_kspace_moments_noalloc", "twmc_debug_philox",
+    "twmc_hbatch_create", "twmc_hbatch_run", "twmc_hbatch_sync", "twmc_hbatch_moments", "twmc_hbatch_state",
+    "twmc_hbatch_plan", "twmc_hbatch_last_error", "twmc_hbatch_launch_count", "twmc_hbatch_destroy",
 ]
 
 
@@ -53,6 +55,15 @@ class TaskDesc(C.Structure):
         ("id", C.c_uint64), ("seed", C.c_uint32), ("ic_kind", C.c_int32), ("t_start", C.c_double),
         ("t_end", C.c_double), ("store_initial", C.c_int32), ("init_field", C.c_void_p),
         ("U_realization", C.c_void_p), ("omega_realization", C.c_void_p), ("F_realization", C.c_void_p),
+    ]
+
+
+class PointDesc(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int64), ("ny", C.c_int64), ("J", C.c_double), ("gamma", C.c_double), ("dt", C.c_double),
+        ("omega", C.c_double * 2), ("U", C.c_double * 2), ("F", C.c_double * 2), ("beta_init", C.c_double * 2),
+        ("beta_init_sigma", C.c_double * 2), ("n_traj", C.c_int64), ("seed0", C.c_uint32), ("id0", C.c_uint64),
+        ("n_moment_blocks", C.c_int32),
     ]
 
 
@@ -97,6 +108,19 @@ def load(path: str = LIB_PATH):
     lib.twmc_stream.argtypes = [C.c_void_p]
     lib.twmc_stream.restype = C.c_void_p
     lib.twmc_measure_fp32_peak.argtypes = [C.POINTER(C.c_double)]
+    lib.twmc_hbatch_create.argtypes = [C.POINTER(PointDesc), C.c_size_t, C.c_int64, C.c_int32, C.POINTER(C.c_void_p)]
+    lib.twmc_hbatch_run.argtypes = [C.c_void_p, C.c_int64]
+    lib.twmc_hbatch_sync.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
+    lib.twmc_hbatch_moments.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.twmc_hbatch_state.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p]
+    lib.twmc_hbatch_plan.argtypes = [C.c_void_p, C.c_size_t]
+    lib.twmc_hbatch_plan.restype = C.c_char_p
+    lib.twmc_hbatch_last_error.argtypes = [C.c_void_p]
+    lib.twmc_hbatch_last_error.restype = C.c_char_p
+    lib.twmc_hbatch_launch_count.argtypes = [C.c_void_p]
+    lib.twmc_hbatch_launch_count.restype = C.c_int64
+    lib.twmc_hbatch_destroy.argtypes = [C.c_void_p]
+    lib.twmc_hbatch_destroy.restype = None
     lib.twmc_kspace_moments_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
                                                 C.c_void_p, C.c_void_p]
     _lib = lib
@@ -282,6 +306,80 @@ class System:
         m = np.zeros((self.n_blocks, self.n_sites, 3), dtype=np.float64) if moments else None
         self._check(self.lib.twmc_batch_download(self.h, _ptr(f), _ptr(m)))
         return f, m
+
+
+def _c2(v):
+    v = complex(v)
+    return (C.c_double * 2)(v.real, v.imag)
+
+
+class HBatch:
+    """Heterogeneous batch of parameter points (twmc_hbatch_*)."""
+
+    def __init__(self, points, frame_steps: int, tune: bool = False):
+        self.lib = load()
+        arr = (PointDesc * len(points))()
+        self.n_sites = []
+        self.n_traj = []
+        self.n_blocks = []
+        for i, p in enumerate(points):
+            d = arr[i]
+            d.nx, d.ny = p.get("nx", 1), p["ny"]
+            d.J, d.gamma, d.dt = p.get("J", 1.0), p.get("gamma", 1.0), p["dt"]
+            d.omega, d.U, d.F = _c2(p.get("omega", 0)), _c2(p.get("U", 0)), _c2(p.get("F", 0))
+            d.beta_init, d.beta_init_sigma = _c2(p.get("beta_init", 0)), _c2(p.get("beta_init_sigma", 0.5))
+            d.n_traj, d.seed0, d.id0 = p["n_traj"], p.get("seed0", 1), p.get("id0", 1)
+            d.n_moment_blocks = p.get("n_moment_blocks", 32)
+            self.n_sites.append(d.nx * d.ny)
+            self.n_traj.append(d.n_traj)
+            self.n_blocks.append(min(d.n_moment_blocks or 32, d.n_traj))
+        h = C.c_void_p()
+        rc = self.lib.twmc_hbatch_create(arr, len(points), frame_steps, int(tune), C.byref(h))
+        self.h = h
+        if rc != OK:
+            msg = self.lib.twmc_hbatch_last_error(h).decode() if h else ""
+            self.close()
+            raise TWMCError(rc, msg)
+
+    def _check(self, rc):
+        if rc != OK:
+            raise TWMCError(rc, self.lib.twmc_hbatch_last_error(self.h).decode())
+
+    def run(self, n_frames: int):
+        self._check(self.lib.twmc_hbatch_run(self.h, n_frames))
+
+    def sync(self) -> float:
+        ms = C.c_double()
+        self._check(self.lib.twmc_hbatch_sync(self.h, C.byref(ms)))
+        return ms.value
+
+    def state(self, i):
+        out = np.zeros((self.n_traj[i], self.n_sites[i]), dtype=np.complex128)
+        self._check(self.lib.twmc_hbatch_state(self.h, i, out.ctypes.data))
+        return out
+
+    def moments(self, i):
+        out = np.zeros((self.n_blocks[i], self.n_sites[i], 3))
+        self._check(self.lib.twmc_hbatch_moments(self.h, i, out.ctypes.data))
+        return out
+
+    def plan(self, i) -> str:
+        return self.lib.twmc_hbatch_plan(self.h, i).decode()
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.twmc_hbatch_launch_count(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.twmc_hbatch_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 def measure_fp32_peak() -> float:

@@ -1,0 +1,85 @@
+"""Heterogeneous batch (one persistent launch per frame, CUDA graph): every
+point must equal the same point run alone through the handle API, bit for
+bit (same device code, same seeds and counters), including the FP64 moment
+blocks; points of shapes without an FFT plan run the real-space kernel in the
+same graph."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from pincosimulator_gb300 import twmc
+
+pytestmark = pytest.mark.gpu
+
+POINTS = [
+    dict(nx=1, ny=32, U=0.3, omega=-1.0, F=1.2, n_traj=300, seed0=10, id0=1),
+    dict(nx=1, ny=256, U=0.1, omega=0.5, F=2.0, n_traj=70, seed0=20, id0=1000),
+    dict(nx=16, ny=16, U=0.2, omega=-0.5, F=1.0, n_traj=37, seed0=30, id0=5000),
+    dict(nx=64, ny=64, U=0.2, omega=-0.5, F=2.0, n_traj=9, seed0=40, id0=9000),
+    dict(nx=32, ny=32, U=0.45, omega=1.5, F=0.3, n_traj=21, seed0=50, id0=1),
+    dict(nx=6, ny=10, U=0.2, omega=0.0, F=1.0, n_traj=13, seed0=60, id0=1),   # no FFT plan: real space
+    dict(nx=1, ny=50, U=0.2, omega=0.0, F=1.0, n_traj=11, seed0=70, id0=1),   # no FFT plan: real space
+]
+DT, FS = 0.002, 50
+
+
+def single(p, frames):
+    hop = twmc.HOP_FFT
+    s = twmc.System(nx=p["nx"], ny=p["ny"], J=1.0, gamma=1.0, dt=DT, frame_steps=FS, omega=p["omega"], U=p["U"],
+                    F=p["F"], beta_init=0.0, beta_init_sigma=0.5, precision=twmc.PREC_F32, hop=hop,
+                    n_moment_blocks=32)
+    s.batch_init(s.make_tasks(p["n_traj"], t_end=1.0, seed0=p["seed0"], id0=p["id0"]))
+    for _ in range(frames):
+        s.advance(FS)
+    s.reduce()
+    s.sync()
+    f, m = s.download(field=True, moments=True)
+    kname = s.kernel_name
+    s.close()
+    return f, m[: min(32, p["n_traj"])], kname
+
+
+def make(points, tune=False):
+    pts = [dict(p, dt=DT) for p in points]
+    return twmc.HBatch(pts, FS, tune=tune)
+
+
+def test_hbatch_matches_single_point_runs(built_lib):
+    hb = make(POINTS)
+    hb.run(3)
+    hb.sync()
+    for i, p in enumerate(POINTS):
+        f, m, kname = single(p, 3)
+        plan = hb.plan(i)
+        assert ("hbatch" in plan) == (kname == "square_fft_kernel"), (plan, kname)
+        st = hb.state(i)
+        assert np.array_equal(st, f), f"point {i} ({plan}): max diff {np.abs(st - f).max()}"
+        hm = hb.moments(i)
+        if kname == "square_fft_kernel":
+            assert np.array_equal(hm, m)
+        else:  # the real-space kernel produces no k-space populations
+            assert np.array_equal(hm[..., :2], m[..., :2])
+    assert hb.launch_count >= 3
+    hb.close()
+
+
+def test_hbatch_autotuner_cache(built_lib, tmp_path, monkeypatch):
+    cache = tmp_path / "tune.json"
+    monkeypatch.setenv("TWMC_TUNE_CACHE", str(cache))
+    hb = make(POINTS[:5], tune=True)
+    hb.run(1)
+    hb.sync()
+    entries = json.loads(cache.read_text())
+    assert len(entries) == 5 and set(entries.values()) <= {"fft", "ell"}
+    for i, p in enumerate(POINTS[:5]):
+        key = [k for k in entries if k.endswith(f"|{p['nx']}x{p['ny']}")][0]
+        assert ("hbatch" in hb.plan(i)) == (entries[key] == "fft")
+        assert np.isfinite(hb.state(i)).all()
+    hb.close()
+    # a second batch reads the cache instead of timing again
+    mtime = os.path.getmtime(cache)
+    hb2 = make(POINTS[:5], tune=True)
+    hb2.close()
+    assert os.path.getmtime(cache) == mtime
