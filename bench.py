@@ -99,12 +99,16 @@ def measured_peaks():
 
 
 def ncu_traffic():
-    """DRAM bytes per step-kernel launch from the committed ncu summary (or None)."""
+    """DRAM bytes per step-kernel launch at the full workload, from the line
+    `dram_bytes_per_launch_full_size: <bytes>` of the committed ncu summary
+    (or None when there is none)."""
+    import re
     try:
-        d = json.load(open(os.path.join(ROOT, "profiles", "square_fft_kernel_64x64.json")))
-        return d.get("dram_bytes_per_launch_full_size")
-    except Exception:
+        txt = open(os.path.join(ROOT, "profiles", "square_fft_kernel_64x64.md")).read()
+    except OSError:
         return None
+    m = re.search(r"dram_bytes_per_launch_full_size:\s*([0-9.eE+]+)", txt)
+    return float(m.group(1)) if m else None
 
 
 def make_system(twmc, hop=None):

@@ -233,6 +233,24 @@ TWMC_API int twmc_hbatch_sync(twmc_hbatch* b, double* ms);
 TWMC_API int twmc_hbatch_moments(twmc_hbatch* b, size_t point, double* out);
 /* Current field of one point (n_traj x sites complex128). */
 TWMC_API int twmc_hbatch_state(twmc_hbatch* b, size_t point, double* out);
+/* Redraws one point's initial fields from per-site device arrays (sites
+ * complex128 each, NULL = the point's uniform value): a = beta_init +
+ * beta_sigma * (xi1 + i xi2) with the same Philox draws as at creation. Only
+ * before the first twmc_hbatch_run (e.g. warm starts from predicted fields). */
+TWMC_API int twmc_hbatch_set_init(twmc_hbatch* b, size_t point, const double* beta_init, const double* beta_sigma);
+/* Trajectory means <a> (complex128) and <|a|^2> (double) per site of every
+ * point into device arrays of twmc_hbatch_total_sites entries (point i's
+ * sites follow point i-1's), FP64 compensated, on the batch's stream
+ * (asynchronous); accumulate != 0 adds to the arrays instead. */
+TWMC_API int twmc_hbatch_field_moments(twmc_hbatch* b, double* mean, double* abs2, int32_t accumulate);
+TWMC_API int64_t twmc_hbatch_total_sites(const twmc_hbatch* b);
+/* Site averages of the last frame's moment blocks of every point into host
+ * out [sum_i n_blocks_i][3] (point i's blocks follow point i-1's): the
+ * inputs of spatially averaged n, g2 with block standard errors per frame,
+ * without copying whole moment arrays. Synchronises. */
+TWMC_API int twmc_hbatch_block_means(twmc_hbatch* b, double* out);
+/* cudaStream_t the batch runs on. */
+TWMC_API void* twmc_hbatch_stream(const twmc_hbatch* b);
 /* Kernel the point runs on. */
 TWMC_API const char* twmc_hbatch_plan(const twmc_hbatch* b, size_t point);
 TWMC_API const char* twmc_hbatch_last_error(const twmc_hbatch* b);
@@ -264,6 +282,66 @@ TWMC_API void twmc_hbatch_destroy(twmc_hbatch* b);
  * ordering) race. The call allocates nothing and does not synchronise. */
 TWMC_API int twmc_kspace_moments_noalloc(const void* state, int64_t n_traj, int64_t nx, int64_t ny,
                                          int32_t n_blocks, double* moments, void* stream);
+
+/* ---- learned warm start --------------------------------------------------- */
+
+/* A multilayer perceptron with BF16 weights and FP32 accumulation on the
+ * tensor cores, GELU after every hidden layer, trained with MSE loss and
+ * Adam. No counterpart in the reference. It maps a parameter point to an
+ * MLP row: (Re a_k, Im a_k) of the steady-state k-mode mean field for every
+ * k (natural order k = kx ny + ky, unitary DFT), then the density n.
+ * Parameters form one FP32 array: for each layer l, W_l [widths[l+1]]
+ * [widths[l]] row-major, then b_l [widths[l+1]]. Pointers named x, y,
+ * target, weights, rows, mean, abs2, beta_* are DEVICE pointers; calls taking
+ * a stream are asynchronous on it. */
+typedef struct twmc_mlp twmc_mlp;
+
+/* widths[0..n_layers]; Glorot-uniform weights from seed, zero biases;
+ * max_batch = rows per backward call (forward calls are chunked). */
+TWMC_API int twmc_mlp_create(int32_t n_layers, const int32_t* widths, int64_t max_batch, uint64_t seed,
+                             twmc_mlp** out);
+TWMC_API int64_t twmc_mlp_param_count(const twmc_mlp* m);
+/* Host copies of the FP32 parameters (set also resets Adam) and gradients. */
+TWMC_API int twmc_mlp_set_params(twmc_mlp* m, const float* host);
+TWMC_API int twmc_mlp_get_params(twmc_mlp* m, float* host);
+TWMC_API int twmc_mlp_get_grads(twmc_mlp* m, float* host);
+/* y [batch][widths[n]] = net(x [batch][widths[0]]). */
+TWMC_API int twmc_mlp_forward(twmc_mlp* m, const float* x, int64_t batch, float* y, void* stream);
+/* Forward + gradients of L = sum_{b,o} w_o (y - target)^2 / (batch O) into
+ * the gradient array (weights: [O] or NULL = 1); *loss (host, optional:
+ * NULL keeps the call asynchronous) receives L. */
+TWMC_API int twmc_mlp_backward(twmc_mlp* m, const float* x, const float* target, const float* weights,
+                               int64_t batch, float* loss, void* stream);
+/* One Adam step from the current gradients. */
+TWMC_API int twmc_mlp_adam(twmc_mlp* m, float lr, float beta1, float beta2, float eps, void* stream);
+/* L of the last backward (synchronises). */
+TWMC_API int twmc_mlp_last_loss(twmc_mlp* m, float* loss);
+TWMC_API const char* twmc_mlp_last_error(const twmc_mlp* m);
+TWMC_API int64_t twmc_mlp_launch_count(const twmc_mlp* m);
+TWMC_API void twmc_mlp_destroy(twmc_mlp* m);
+/* Prepares training rows t [rows][cols] in place: squash each value to
+ * asinh(v / squash) when squash > 0 (log-like beyond |v| ~ squash), then
+ * standardise every column (mean, stdv per column; the deviation floored at
+ * floor_frac x its maximum over columns). weights (optional, [cols]): loss
+ * weights clamp((stdv_c / max stdv)^2, 1e-4, 1) from the unfloored
+ * deviations, so columns that barely vary across points (k-modes that vanish
+ * by symmetry, up to noise) do not dominate the loss. */
+TWMC_API int twmc_mlp_standardize(float* t, int64_t rows, int32_t cols, double squash, float floor_frac, float* mean,
+                                  float* stdv, float* weights, void* stream);
+/* MLP rows [n_points][ld] (ld >= 2 nx ny + 1) from per-point sums over
+ * `frames` frames of the mean field (complex128, [n_points][nx ny]) and of
+ * <|a|^2> ([n_points][nx ny]), e.g. from twmc_hbatch_field_moments. */
+TWMC_API int twmc_mlp_targets(const double* mean, const double* abs2, int64_t n_points, int64_t nx, int64_t ny,
+                              int32_t frames, float* rows, int64_t ld, void* stream);
+/* Initial fields from MLP rows (de-standardised with mean / stdv when not
+ * NULL, then un-squashed with squash as above): beta_init = inverse DFT of
+ * the predicted amplitudes, beta_sigma = sqrt((n_inc + 1/2) / 2) per
+ * quadrature with n_inc = min(max(n - |beta_init|^2, 0), max_incoherent)
+ * (complex128, [n_points][nx ny] each), the inputs of twmc_hbatch_set_init.
+ * nx ny <= 4096. */
+TWMC_API int twmc_mlp_fields(const float* rows, int64_t ld, int64_t n_points, const float* mean, const float* stdv,
+                             double squash, double max_incoherent, int64_t nx, int64_t ny, double* beta_init,
+                             double* beta_sigma, void* stream);
 
 /* ---- self-check entry points -------------------------------------------- */
 

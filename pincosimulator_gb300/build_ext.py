@@ -22,7 +22,8 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompiler", "-fPIC",
          "-Xcompiler", "-fvisibility=hidden", "-DNDEBUG", "-I", os.path.join(HERE, "..", "include")]
 SOURCES = ["twmc_api.cu", "twmc_square_f32.cu", "twmc_square_f64.cu", "twmc_ell.cu", "twmc_misc.cu",
-           "twmc_noalloc.cu", "twmc_hbatch.cu"]
+           "twmc_noalloc.cu", "twmc_hbatch.cu",
+           "twmc_mlp.cu"]
 
 
 def _write_plans() -> None:

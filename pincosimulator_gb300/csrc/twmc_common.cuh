@@ -17,6 +17,12 @@ template <typename R> using c2_t = typename C2<R>::type;
 template <typename T> __device__ __forceinline__ T cmake(decltype(T::x) x, decltype(T::x) y) { T r; r.x = x; r.y = y; return r; }
 template <typename T> __device__ __forceinline__ T cadd(T a, T b) { return cmake<T>(a.x + b.x, a.y + b.y); }
 template <typename T> __device__ __forceinline__ T csub(T a, T b) { return cmake<T>(a.x - b.x, a.y - b.y); }
+// FP32 complex add/sub as one packed FP32x2 instruction (sm_100+); same
+// round-to-nearest results as the two scalar operations.
+template <> __device__ __forceinline__ float2 cadd<float2>(float2 a, float2 b) { return __fadd2_rn(a, b); }
+template <> __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b) {
+  return __fadd2_rn(a, make_float2(-b.x, -b.y));
+}
 template <typename T> __device__ __forceinline__ T cmul(T a, T b) { return cmake<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 // a * conj(b)
 template <typename T> __device__ __forceinline__ T cmulc(T a, T b) { return cmake<T>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }

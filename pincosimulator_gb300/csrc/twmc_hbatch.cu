@@ -136,6 +136,57 @@ __global__ void hbatch_moments_kernel(const MomentArgs* __restrict__ ma) {
   moments_site<float>(a, p, int(blockIdx.y));
 }
 
+// Trajectory means of a and |a|^2 per site of every point, FP64 compensated,
+// in trajectory order: grid (site chunk, point). Point i's sites start at
+// site_off[i] in mean (complex) and abs2.
+__global__ void hbatch_field_kernel(const MomentArgs* __restrict__ ma, const int64_t* __restrict__ site_off,
+                                    double* __restrict__ mean, double* __restrict__ abs2, int accumulate) {
+  const MomentArgs& a = ma[blockIdx.y];
+  const int64_t p = blockIdx.x * int64_t(blockDim.x) + threadIdx.x;
+  if (p >= a.nsites) return;
+  const float2* st = reinterpret_cast<const float2*>(a.state);
+  KSum sr, si, s2;
+  for (int64_t tr = 0; tr < a.ntraj; ++tr) {
+    const float2 v = st[tr * a.nsites + p];
+    sr.add(double(v.x));
+    si.add(double(v.y));
+    s2.add(double(v.x) * double(v.x) + double(v.y) * double(v.y));
+  }
+  const double inv = 1.0 / double(a.ntraj);
+  const int64_t o = site_off[blockIdx.y] + p;
+  const double mr = sr.value() * inv, mi = si.value() * inv, m2 = s2.value() * inv;
+  mean[2 * o] = accumulate ? mean[2 * o] + mr : mr;
+  mean[2 * o + 1] = accumulate ? mean[2 * o + 1] + mi : mi;
+  abs2[o] = accumulate ? abs2[o] + m2 : m2;
+}
+
+// Site averages of every moment block: out[(blk_off[i] + b) * 3 + c] =
+// mean over sites of moments[i][b][site][c]; grid (block, point), FP64.
+__global__ void hbatch_block_means_kernel(const MomentArgs* __restrict__ ma, const int64_t* __restrict__ blk_off,
+                                          double* __restrict__ out) {
+  const MomentArgs& a = ma[blockIdx.y];
+  const int b = blockIdx.x;
+  if (b >= a.nblocks) return;
+  double s[3] = {0.0, 0.0, 0.0};
+  for (int64_t p = threadIdx.x; p < a.nsites; p += blockDim.x)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) s[c] += a.out[(int64_t(b) * a.nsites + p) * 3 + c];
+  __shared__ double red[3][32];
+#pragma unroll
+  for (int c = 0; c < 3; ++c) {
+    double v = s[c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if ((threadIdx.x & 31) == 0) red[c][threadIdx.x >> 5] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < 3) {
+    double v = 0.0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) v += red[threadIdx.x][w];
+    out[(blk_off[blockIdx.y] + b) * 3 + threadIdx.x] = v / double(a.nsites);
+  }
+}
+
 __global__ void hbatch_bump_kernel(StepArgs* pts, int n, uint32_t steps) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) pts[i].step0 += steps;
@@ -222,6 +273,12 @@ struct twmc_hbatch {
   DBuf<MomentArgs> margs;
   DBuf<double> moments;
   std::vector<int64_t> mom_off;
+  std::vector<int64_t> traj_off;   // first trajectory of each point in seeds / ids / status
+  DBuf<int64_t> site_off;          // first site of each point in the per-site outputs
+  int64_t total_sites = 0;
+  DBuf<int64_t> blk_off;           // first moment block of each point in the block-mean output
+  DBuf<double> blk_means;
+  int64_t total_blocks = 0;
   int nitems = 0, grid = 0;
   int64_t max_sites = 0;
   int max_blocks = 0;
@@ -236,6 +293,33 @@ namespace {
 int hfail(twmc_hbatch* b, int code, const std::string& m) {
   b->err = m;
   return code;
+}
+
+// Draws the initial fields of point i (ReadFromSettings): beta_init +
+// beta_init_sigma * xi per site, from the per-site device arrays binit /
+// bsigma ([sites] complex128) where given, else the point's uniform values.
+bool init_point(twmc_hbatch* b, size_t i, const double* binit, const double* bsigma, std::string* e) {
+  const twmc_point_desc& p = b->desc[i];
+  InitArgs ia;
+  std::memset(&ia, 0, sizeof(ia));
+  ia.ntraj = b->ntraj[i];
+  ia.nsites = b->nsites[i];
+  ia.prec = 0;
+  ia.state = b->state.p + b->off_state[i];
+  ia.seeds = b->seeds.p + b->traj_off[i];
+  ia.ids = b->ids.p + b->traj_off[i];
+  ia.ic_kind = TWMC_IC_SETTINGS;
+  ia.binit = binit;
+  ia.bsigma = bsigma;
+  ia.binit_s[0] = p.beta_init[0];
+  ia.binit_s[1] = p.beta_init[1];
+  ia.bsigma_s[0] = p.beta_init_sigma[0];
+  ia.bsigma_s[1] = p.beta_init_sigma[1];
+  ia.lattice = 0;
+  ia.gamma = p.gamma;
+  if (!init_launch(ia, b->s0, e)) return false;
+  ++b->launches;
+  return true;
 }
 
 int lg2(int64_t v) {
@@ -390,6 +474,16 @@ int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_st
   }
   b->max_sites = max_sites;
   b->max_blocks = max_blocks;
+  std::vector<int64_t> soff(n);
+  b->total_sites = 0;
+  for (size_t i = 0; i < n; ++i) { soff[i] = b->total_sites; b->total_sites += b->nsites[i]; }
+  std::vector<int64_t> boff(n);
+  b->total_blocks = 0;
+  for (size_t i = 0; i < n; ++i) { boff[i] = b->total_blocks; b->total_blocks += b->nblocks[i]; }
+  if (!b->site_off.alloc(n) || !b->blk_off.alloc(n) || !b->blk_means.alloc(size_t(b->total_blocks) * 3))
+    return hfail(b, TWMC_ERR_NOMEM, "device allocation failed");
+  cudaMemcpy(b->site_off.p, soff.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice);
+  cudaMemcpy(b->blk_off.p, boff.data(), n * sizeof(int64_t), cudaMemcpyHostToDevice);
   int64_t trajs = 0;
   for (size_t i = 0; i < n; ++i) trajs += b->ntraj[i];
   if (!b->state.alloc(size_t(total)) || !b->nk.alloc(size_t(total)) || !b->seeds.alloc(size_t(trajs)) ||
@@ -399,7 +493,9 @@ int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_st
   // tables per point: twiddles [M0 + M1], separable k table [M0 + M1] (dt folded in)
   std::vector<float2> tw;
   std::vector<float> kt;
-  std::vector<int64_t> tw_off(n), traj_off(n);
+  std::vector<int64_t> tw_off(n);
+  std::vector<int64_t>& traj_off = b->traj_off;
+  traj_off.assign(n, 0);
   std::vector<uint32_t> hseeds(static_cast<size_t>(trajs)), hids(static_cast<size_t>(trajs));
   int64_t to = 0;
   for (size_t i = 0; i < n; ++i) {
@@ -475,24 +571,8 @@ int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_st
 
   // initial fields (ReadFromSettings with uniform beta_init / sigma)
   for (size_t i = 0; i < n; ++i) {
-    InitArgs ia;
-    std::memset(&ia, 0, sizeof(ia));
-    ia.ntraj = b->ntraj[i];
-    ia.nsites = b->nsites[i];
-    ia.prec = 0;
-    ia.state = b->state.p + b->off_state[i];
-    ia.seeds = b->seeds.p + traj_off[i];
-    ia.ids = b->ids.p + traj_off[i];
-    ia.ic_kind = TWMC_IC_SETTINGS;
-    ia.binit_s[0] = points[i].beta_init[0];
-    ia.binit_s[1] = points[i].beta_init[1];
-    ia.bsigma_s[0] = points[i].beta_init_sigma[0];
-    ia.bsigma_s[1] = points[i].beta_init_sigma[1];
-    ia.lattice = 0;
-    ia.gamma = points[i].gamma;
     std::string e;
-    if (!init_launch(ia, b->s0, &e)) return hfail(b, TWMC_ERR_CUDA, e);
-    ++b->launches;
+    if (!init_point(b, i, nullptr, nullptr, &e)) return hfail(b, TWMC_ERR_CUDA, e);
   }
 
   // persistent kernel configuration
@@ -581,6 +661,41 @@ int twmc_hbatch_state(twmc_hbatch* b, size_t point, double* out) {
   for (size_t k = 0; k < cnt; ++k) { out[2 * k] = tmp[k].x; out[2 * k + 1] = tmp[k].y; }
   return TWMC_OK;
 }
+
+int twmc_hbatch_set_init(twmc_hbatch* b, size_t point, const double* beta_init, const double* beta_sigma) {
+  if (!b || point >= b->npts) return TWMC_ERR_INVALID;
+  if (b->frames_run > 0) return hfail(b, TWMC_ERR_INVALID, "initial fields can only be set before the first run");
+  cudaSetDevice(b->device);
+  std::string e;
+  if (!init_point(b, point, beta_init, beta_sigma, &e)) return hfail(b, TWMC_ERR_CUDA, e);
+  return TWMC_OK;
+}
+
+int twmc_hbatch_field_moments(twmc_hbatch* b, double* mean, double* abs2, int32_t accumulate) {
+  if (!b || !mean || !abs2) return TWMC_ERR_INVALID;
+  cudaSetDevice(b->device);
+  dim3 g(unsigned((b->max_sites + 127) / 128), unsigned(b->npts));
+  hbatch_field_kernel<<<g, 128, 0, b->s0>>>(b->margs.p, b->site_off.p, mean, abs2, accumulate ? 1 : 0);
+  ++b->launches;
+  cudaError_t ce = cudaGetLastError();
+  return ce == cudaSuccess ? TWMC_OK : hfail(b, TWMC_ERR_CUDA, cudaGetErrorString(ce));
+}
+
+int64_t twmc_hbatch_total_sites(const twmc_hbatch* b) { return b ? b->total_sites : -1; }
+
+int twmc_hbatch_block_means(twmc_hbatch* b, double* out) {
+  if (!b || !out) return TWMC_ERR_INVALID;
+  cudaSetDevice(b->device);
+  dim3 g(unsigned(b->max_blocks), unsigned(b->npts));
+  hbatch_block_means_kernel<<<g, 128, 0, b->s0>>>(b->margs.p, b->blk_off.p, b->blk_means.p);
+  ++b->launches;
+  cudaError_t e = cudaMemcpyAsync(out, b->blk_means.p, size_t(b->total_blocks) * 3 * sizeof(double),
+                                  cudaMemcpyDeviceToHost, b->s0);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->s0);
+  return e == cudaSuccess ? TWMC_OK : hfail(b, TWMC_ERR_CUDA, cudaGetErrorString(e));
+}
+
+void* twmc_hbatch_stream(const twmc_hbatch* b) { return b ? static_cast<void*>(b->s0) : nullptr; }
 
 const char* twmc_hbatch_plan(const twmc_hbatch* b, size_t point) {
   if (!b || point >= b->npts) return "";

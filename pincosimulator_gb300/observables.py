@@ -67,17 +67,23 @@ def observables(moments: np.ndarray, ntraj: int) -> dict:
             "bm2": bm2}
 
 
-def time_to_steady_state(times: np.ndarray, nbar: np.ndarray, nbar_se: np.ndarray, tail: float = 0.25):
-    """Earliest save time after which the spatially averaged n stays within
-    max(1 SE, 1e-3 n_inf) of n_inf, n_inf = mean of the last `tail` of the frames."""
+def time_to_steady_state(times: np.ndarray, nbar: np.ndarray, nbar_se: np.ndarray, tail: float = 0.25,
+                         hold: int = 2):
+    """Earliest save time at which the spatially averaged n is within
+    max(1 SE, 1e-3 n_inf) of n_inf (the mean of the last `tail` of the
+    frames) and stays within twice that band for the next `hold` frames.
+
+    First entry rather than "never leaves again": with a one-SE band, noise
+    alone takes about a third of the steady frames outside it. Returns
+    (time, n_inf); the last save time if the band is never reached."""
     times = np.asarray(times)
     nbar = np.asarray(nbar)
     k0 = int(np.floor((1.0 - tail) * len(nbar)))
     n_inf = float(np.mean(nbar[k0:]))
-    tol = np.maximum(np.asarray(nbar_se), 1e-3 * abs(n_inf))
-    ok = np.abs(nbar - n_inf) <= tol
-    # last frame that violates the band; steady from the next one on
-    bad = np.nonzero(~ok)[0]
-    k = 0 if len(bad) == 0 else int(bad[-1]) + 1
-    k = min(k, len(times) - 1)
-    return float(times[k]), n_inf
+    tol = np.maximum(np.asarray(nbar_se), 1e-3 * abs(n_inf)) * np.ones_like(nbar)
+    dev = np.abs(nbar - n_inf)
+    for k in range(len(nbar)):
+        nxt = slice(k + 1, min(len(nbar), k + 1 + hold))
+        if dev[k] <= tol[k] and np.all(dev[nxt] <= 2.0 * tol[nxt]):
+            return float(times[k]), n_inf
+    return float(times[-1]), n_inf

@@ -32,6 +32,11 @@ EXPORTED = [
     "twmc_kspace_moments_noalloc", "twmc_debug_philox",
     "twmc_hbatch_create", "twmc_hbatch_run", "twmc_hbatch_sync", "twmc_hbatch_moments", "twmc_hbatch_state",
     "twmc_hbatch_plan", "twmc_hbatch_last_error", "twmc_hbatch_launch_count", "twmc_hbatch_destroy",
+    "twmc_hbatch_set_init", "twmc_hbatch_field_moments", "twmc_hbatch_total_sites", "twmc_hbatch_stream",
+    "twmc_hbatch_block_means",
+    "twmc_mlp_create", "twmc_mlp_param_count", "twmc_mlp_set_params", "twmc_mlp_get_params", "twmc_mlp_get_grads",
+    "twmc_mlp_forward", "twmc_mlp_backward", "twmc_mlp_adam", "twmc_mlp_last_loss", "twmc_mlp_last_error",
+    "twmc_mlp_launch_count", "twmc_mlp_destroy", "twmc_mlp_standardize", "twmc_mlp_targets", "twmc_mlp_fields",
 ]
 
 
@@ -78,11 +83,12 @@ class Outputs(C.Structure):
 _lib = None
 
 
-def load(path: str = LIB_PATH):
-    """Loads the C-ABI library; raises if it has not been built."""
+def load(path: Optional[str] = None):
+    """Loads the C-ABI library ($TWMC_LIB if set); raises if it has not been built."""
     global _lib
     if _lib is not None:
         return _lib
+    path = path or os.environ.get("TWMC_LIB") or LIB_PATH
     if not os.path.exists(path):
         raise RuntimeError(f"libtwmc_cuda.so not built ({path}); run __graft_entry__.build()")
     lib = C.CDLL(path)
@@ -123,6 +129,34 @@ def load(path: str = LIB_PATH):
     lib.twmc_hbatch_destroy.restype = None
     lib.twmc_kspace_moments_noalloc.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
                                                 C.c_void_p, C.c_void_p]
+    lib.twmc_hbatch_set_init.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]
+    lib.twmc_hbatch_field_moments.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32]
+    lib.twmc_hbatch_total_sites.argtypes = [C.c_void_p]
+    lib.twmc_hbatch_total_sites.restype = C.c_int64
+    lib.twmc_hbatch_block_means.argtypes = [C.c_void_p, C.c_void_p]
+    lib.twmc_hbatch_stream.argtypes = [C.c_void_p]
+    lib.twmc_hbatch_stream.restype = C.c_void_p
+    lib.twmc_mlp_create.argtypes = [C.c_int32, C.c_void_p, C.c_int64, C.c_uint64, C.POINTER(C.c_void_p)]
+    lib.twmc_mlp_param_count.argtypes = [C.c_void_p]
+    lib.twmc_mlp_param_count.restype = C.c_int64
+    for f in ("twmc_mlp_set_params", "twmc_mlp_get_params", "twmc_mlp_get_grads", "twmc_mlp_last_loss"):
+        getattr(lib, f).argtypes = [C.c_void_p, C.c_void_p]
+    lib.twmc_mlp_forward.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]
+    lib.twmc_mlp_backward.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int64, C.c_void_p,
+                                      C.c_void_p]
+    lib.twmc_mlp_adam.argtypes = [C.c_void_p, C.c_float, C.c_float, C.c_float, C.c_float, C.c_void_p]
+    lib.twmc_mlp_last_error.argtypes = [C.c_void_p]
+    lib.twmc_mlp_last_error.restype = C.c_char_p
+    lib.twmc_mlp_launch_count.argtypes = [C.c_void_p]
+    lib.twmc_mlp_launch_count.restype = C.c_int64
+    lib.twmc_mlp_destroy.argtypes = [C.c_void_p]
+    lib.twmc_mlp_destroy.restype = None
+    lib.twmc_mlp_standardize.argtypes = [C.c_void_p, C.c_int64, C.c_int32, C.c_double, C.c_float, C.c_void_p,
+                                         C.c_void_p, C.c_void_p, C.c_void_p]
+    lib.twmc_mlp_targets.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_int64, C.c_int32,
+                                     C.c_void_p, C.c_int64, C.c_void_p]
+    lib.twmc_mlp_fields.argtypes = [C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_double,
+                                    C.c_double, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p]
     _lib = lib
     return lib
 
@@ -367,6 +401,36 @@ class HBatch:
         return self.lib.twmc_hbatch_plan(self.h, i).decode()
 
     @property
+    def stream(self) -> int:
+        """cudaStream_t of the batch (for torch.cuda.ExternalStream)."""
+        return int(self.lib.twmc_hbatch_stream(self.h) or 0)
+
+    @property
+    def total_sites(self) -> int:
+        return int(self.lib.twmc_hbatch_total_sites(self.h))
+
+    def set_init(self, i, beta_init_ptr: int, beta_sigma_ptr: int):
+        """Redraws point i's initial fields from per-site device arrays
+        (complex128, sites each; 0 = the point's uniform value). Before run()."""
+        self._check(self.lib.twmc_hbatch_set_init(self.h, i, beta_init_ptr or None, beta_sigma_ptr or None))
+
+    def block_means(self):
+        """Per point: (n_blocks, 3) site averages of the last frame's moment blocks."""
+        tot = sum(self.n_blocks)
+        out = np.zeros((tot, 3))
+        self._check(self.lib.twmc_hbatch_block_means(self.h, out.ctypes.data))
+        res, o = [], 0
+        for nb in self.n_blocks:
+            res.append(out[o:o + nb])
+            o += nb
+        return res
+
+    def field_moments(self, mean_ptr: int, abs2_ptr: int, accumulate: bool = False):
+        """Trajectory means <a> (complex128) and <|a|^2> per site of every point
+        into device arrays of total_sites entries (asynchronous on `stream`)."""
+        self._check(self.lib.twmc_hbatch_field_moments(self.h, mean_ptr, abs2_ptr, int(accumulate)))
+
+    @property
     def launch_count(self) -> int:
         return int(self.lib.twmc_hbatch_launch_count(self.h))
 
@@ -380,6 +444,110 @@ class HBatch:
             self.close()
         except Exception:
             pass
+
+
+class MLP:
+    """BF16 tensor-core MLP of the learned warm start (twmc_mlp_*). Arrays
+    passed to forward / backward are device pointers (e.g. torch tensors'
+    data_ptr()); parameters and gradients come back as host FP32 arrays."""
+
+    def __init__(self, widths: Sequence[int], max_batch: int, seed: int = 1):
+        self.lib = load()
+        self.widths = [int(w) for w in widths]
+        w = (C.c_int32 * len(self.widths))(*self.widths)
+        h = C.c_void_p()
+        rc = self.lib.twmc_mlp_create(len(self.widths) - 1, w, int(max_batch), int(seed), C.byref(h))
+        self.h = h
+        if rc != OK:
+            msg = self.lib.twmc_mlp_last_error(h).decode() if h else ""
+            self.close()
+            raise TWMCError(rc, msg)
+        self.max_batch = int(max_batch)
+        self.n_params = int(self.lib.twmc_mlp_param_count(self.h))
+
+    def _check(self, rc):
+        if rc != OK:
+            raise TWMCError(rc, self.lib.twmc_mlp_last_error(self.h).decode())
+
+    def offsets(self):
+        """[(w_off, b_off)] per layer into the parameter array."""
+        out, off = [], 0
+        for k, n in zip(self.widths[:-1], self.widths[1:]):
+            out.append((off, off + n * k))
+            off += n * k + n
+        return out
+
+    def get_params(self) -> np.ndarray:
+        out = np.zeros(self.n_params, dtype=np.float32)
+        self._check(self.lib.twmc_mlp_get_params(self.h, out.ctypes.data))
+        return out
+
+    def set_params(self, p: np.ndarray):
+        p = np.ascontiguousarray(p, dtype=np.float32)
+        assert p.size == self.n_params
+        self._check(self.lib.twmc_mlp_set_params(self.h, p.ctypes.data))
+
+    def get_grads(self) -> np.ndarray:
+        out = np.zeros(self.n_params, dtype=np.float32)
+        self._check(self.lib.twmc_mlp_get_grads(self.h, out.ctypes.data))
+        return out
+
+    def forward(self, x_ptr: int, batch: int, y_ptr: int, stream: int = 0):
+        self._check(self.lib.twmc_mlp_forward(self.h, x_ptr, int(batch), y_ptr, stream or None))
+
+    def backward(self, x_ptr: int, t_ptr: int, batch: int, w_ptr: int = 0, stream: int = 0, want_loss=False):
+        loss = C.c_float(0.0)
+        self._check(self.lib.twmc_mlp_backward(self.h, x_ptr, t_ptr, w_ptr or None, int(batch),
+                                               C.byref(loss) if want_loss else None, stream or None))
+        return float(loss.value) if want_loss else None
+
+    def adam(self, lr: float, beta1: float = 0.9, beta2: float = 0.999, eps: float = 1e-8, stream: int = 0):
+        self._check(self.lib.twmc_mlp_adam(self.h, lr, beta1, beta2, eps, stream or None))
+
+    def last_loss(self) -> float:
+        v = C.c_float()
+        self._check(self.lib.twmc_mlp_last_loss(self.h, C.byref(v)))
+        return float(v.value)
+
+    @property
+    def launch_count(self) -> int:
+        return int(self.lib.twmc_mlp_launch_count(self.h))
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.twmc_mlp_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def mlp_standardize(t_ptr: int, rows: int, cols: int, floor_frac: float, mean_ptr: int, std_ptr: int,
+                    squash: float = 0.0, weights_ptr: int = 0, stream: int = 0):
+    rc = load().twmc_mlp_standardize(t_ptr, int(rows), int(cols), float(squash), float(floor_frac), mean_ptr,
+                                     std_ptr, weights_ptr or None, stream or None)
+    if rc != OK:
+        raise TWMCError(rc, "twmc_mlp_standardize failed")
+
+
+def mlp_targets(mean_ptr: int, abs2_ptr: int, n_points: int, nx: int, ny: int, frames: int, rows_ptr: int,
+                ld: int, stream: int = 0):
+    rc = load().twmc_mlp_targets(mean_ptr, abs2_ptr, int(n_points), int(nx), int(ny), int(frames), rows_ptr,
+                                 int(ld), stream or None)
+    if rc != OK:
+        raise TWMCError(rc, "twmc_mlp_targets failed")
+
+
+def mlp_fields(rows_ptr: int, ld: int, n_points: int, mean_ptr: int, std_ptr: int, nx: int, ny: int,
+               binit_ptr: int, bsigma_ptr: int, squash: float = 0.0, max_incoherent: float = 1e30, stream: int = 0):
+    rc = load().twmc_mlp_fields(rows_ptr, int(ld), int(n_points), mean_ptr or None, std_ptr or None,
+                                float(squash), float(max_incoherent), int(nx), int(ny), binit_ptr, bsigma_ptr,
+                                stream or None)
+    if rc != OK:
+        raise TWMCError(rc, "twmc_mlp_fields failed")
 
 
 def measure_fp32_peak() -> float:
