@@ -12,7 +12,10 @@ all 16384 trajectories (on-chip FFT hopping) plus the FP64 reduction of the
 frame's moments. The state (512 MB) is larger than L2, so every launch
 streams it from HBM.
 
-Metric: site-updates/s (sites x steps x trajectories per second).
+Metric: site-updates/s (sites x steps x trajectories per second), and, as
+the second half of the headline metric, time to steady state with and
+without the learned warm start on a reduced 32 x 32 parameter sweep
+(`time_to_steady_state`; skip with --no-warm).
 
   python bench.py [--gpus N --steps K --warmup W]          this engine
   python bench.py --impl reference [...]                   the CPU arm
@@ -98,17 +101,64 @@ def measured_peaks():
         return {}
 
 
-def ncu_traffic():
-    """DRAM bytes per step-kernel launch at the full workload, from the line
-    `dram_bytes_per_launch_full_size: <bytes>` of the committed ncu summary
-    (or None when there is none)."""
+def _profile_figure(key):
+    """A figure `key: <number>` from the committed ncu summary of the step
+    kernel (profiles/square_fft_kernel_64x64.md), or None."""
     import re
     try:
         txt = open(os.path.join(ROOT, "profiles", "square_fft_kernel_64x64.md")).read()
     except OSError:
         return None
-    m = re.search(r"dram_bytes_per_launch_full_size:\s*([0-9.eE+]+)", txt)
+    m = re.search(re.escape(key) + r":\s*([0-9.eE+]+)", txt)
     return float(m.group(1)) if m else None
+
+
+def ncu_traffic():
+    """DRAM bytes per step-kernel launch at the full workload (ncu, scaled from the small capture)."""
+    return _profile_figure("dram_bytes_per_launch_full_size")
+
+
+def measure_warm_start(n_train=1024, traj_train=256, t_train=20.0, n_test=64, traj_test=512, t_test=20.0):
+    """Time to steady state with and without the learned warm start on a
+    reduced version of the 32 x 32 sweep (F ~ U[0,3], detuning ~ U[-2,2],
+    U ~ U[0.05,0.5], J = gamma = 1, dt = 0.002): plain runs of n_train points
+    generate the training rows, the MLP is trained on the GPU, then n_test
+    held-out points run warm-started and plain (the judge)."""
+    import numpy as np
+    import torch
+    from pincosimulator_gb300 import warmstart as wsm
+
+    t0 = time.perf_counter()
+    train = wsm.sample_points(n_train, seed=101)
+    rows, su = wsm.steady_rows(train, 32, 32, n_traj=traj_train, t_end=t_train)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ws = wsm.WarmStart(32, 32, max_batch=128, seed=7)
+    rep = ws.fit(wsm.features(train), rows, epochs=2000, batch=128, lr=3e-3)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    test = wsm.sample_points(n_test, seed=202)
+    res = wsm.warm_sweep(ws, test, n_traj=traj_test, t_end=t_test)
+    t3 = time.perf_counter()
+    tw, tp = float(np.median(res.warm.ttss)), float(np.median(res.plain.ttss))
+    se_n = np.sqrt(res.warm.n_inf_se ** 2 + res.plain.n_inf_se ** 2)
+    se_g = np.sqrt(res.warm.g2_inf_se ** 2 + res.plain.g2_inf_se ** 2)
+    ok = np.isfinite(se_g) & np.isfinite(res.warm.g2_inf)
+    return {
+        "workload": f"32x32 PBC sweep, train {n_train} points x {traj_train} trajectories to t={t_train:g}, "
+                    f"test {n_test} held-out points x {traj_test} trajectories to t={t_test:g}, dt=0.002, "
+                    "frames every 0.5; MLP 5-256-256-256-2049 BF16, 2000 epochs",
+        "ttss_plain_median": tp, "ttss_warm_median": tw, "speedup_median": tp / max(tw, 0.5),
+        "ttss_plain_mean": float(np.mean(res.plain.ttss)), "ttss_warm_mean": float(np.mean(res.warm.ttss)),
+        "n_within_1se_frac": float(np.mean(np.abs(res.warm.n_inf - res.plain.n_inf) <= se_n)),
+        "g2_within_1se_frac": float(np.mean(np.abs(res.warm.g2_inf - res.plain.g2_inf)[ok] <= se_g[ok]))
+        if ok.any() else None,
+        "reruns": int(res.rerun.sum()), "test_points": n_test,
+        "train_s": t1 - t0, "train_site_updates_per_s": su / (t1 - t0), "fit_s": t2 - t1,
+        "fit_steps": rep.steps, "mlp_launches": rep.launches, "final_loss": rep.losses[-1][1], "sweep_s": t3 - t2,
+        "ttss_definition": "first save time with |n - n_inf| <= max(1 SE, 1e-3 n_inf), staying within 2x for "
+                           "2 more frames; n_inf = mean of the last quarter of frames",
+    }
 
 
 def make_system(twmc, hop=None):
@@ -186,6 +236,7 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-warm", action="store_true", help="skip the learned warm-start time-to-steady-state leg")
     ap.add_argument("--ntraj", type=int, default=NTRAJ, help="profiling cases only; the bench line uses 16384")
     args = ap.parse_args()
     rank, world, local = env_rank()
@@ -275,7 +326,19 @@ def main():
             dist.destroy_process_group()
         return 0
     peaks = measured_peaks()
+    # instruction-issue roofline: ncu's instructions per site-update x the
+    # measured rate, against one warp instruction per cycle per scheduler
+    ipsu = _profile_figure("inst_per_site_update")
+    issue = None
+    if ipsu and clocks and clocks.get("sm_mhz"):
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        ach = su_rank / (kernel_ms / 1e3) * ipsu / 32.0
+        pk = sms * 4 * clocks["sm_mhz"] * 1e6
+        issue = {"inst_per_site_update": ipsu, "achieved_warp_inst_per_s": ach, "peak_warp_inst_per_s": pk,
+                 "frac": ach / pk, "source": "ncu instruction count (profiles/square_fft_kernel_64x64.md) x "
+                 "measured rate; peak = SMs x 4 schedulers x median SM clock"}
     cpu = None if (args.no_cpu_baseline or world > 1) else cpu_baseline()
+    warm = None if (args.no_warm or world > 1) else measure_warm_start()
     hbm = peaks.get("hbm_gbs")
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -288,9 +351,9 @@ def main():
                      "flops_per_site_update": FLOPS_PER_SITE_UPDATE,
                      "hbm": {"achieved_gbs": su_rank * BYTES_PER_SITE_UPDATE_HBM / (kernel_ms / 1e3) / 1e9,
                              "peak_gbs": hbm, "source": "MEASURED_PEAKS.json" if hbm else None}},
-        "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu, "clocks": clocks,
+        "issue": issue, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu, "clocks": clocks,
         "trajectories_per_s": value / (NX * NY * (T_END / DT)), "finite": finite,
-        "kernel_ms": kernel_ms,
+        "kernel_ms": kernel_ms, "time_to_steady_state": warm,
     }
     print(json.dumps(line), flush=True)
     if dist:
