@@ -161,11 +161,33 @@ def measure_warm_start(n_train=1024, traj_train=256, t_train=20.0, n_test=64, tr
     }
 
 
-def make_system(twmc, hop=None):
+def make_system(twmc, hop=None, precision=None):
     return twmc.System(nx=NX, ny=NY, J=1.0, gamma=1.0, dt=DT, frame_steps=FRAME_STEPS,
                        omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=0.2, F=2.0, beta_init=0.0,
-                       beta_init_sigma=0.5, precision=twmc.PREC_F32,
+                       beta_init_sigma=0.5, precision=twmc.PREC_F32 if precision is None else precision,
                        hop=twmc.HOP_FFT if hop is None else hop, n_moment_blocks=32)
+
+
+def measure_f64(twmc, torch, steps=2):
+    """The same workload in the engine's FP64 mode (FP64 state, FFT and noise:
+    the plain FP64 GPU split-step), device-timed like the headline."""
+    sysd = make_system(twmc, precision=twmc.PREC_F64)
+    sysd.batch_init(sysd.make_tasks(NTRAJ, t_start=0.0, t_end=T_END, seed0=3, id0=1))
+    sysd.advance(FRAME_STEPS)
+    sysd.sync()
+    ext = torch.cuda.ExternalStream(sysd.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(steps):
+        sysd.advance(FRAME_STEPS)
+        sysd.reduce()
+    e1.record(ext)
+    sysd.sync()
+    ms = e0.elapsed_time(e1)
+    kname = sysd.kernel_name
+    sysd.close()
+    return {"value": steps * FRAME_STEPS * NTRAJ * NX * NY / (ms / 1e3), "unit": METRIC, "steps": steps,
+            "kernel": kname}
 
 
 def cpu_baseline(target_s=12.0, threads=None):
@@ -237,6 +259,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm-start time-to-steady-state leg")
+    ap.add_argument("--no-f64", action="store_true", help="skip timing the FP64 mode")
     ap.add_argument("--ntraj", type=int, default=NTRAJ, help="profiling cases only; the bench line uses 16384")
     args = ap.parse_args()
     rank, world, local = env_rank()
@@ -339,6 +362,10 @@ def main():
                  "measured rate; peak = SMs x 4 schedulers x median SM clock"}
     cpu = None if (args.no_cpu_baseline or world > 1) else cpu_baseline()
     warm = None if (args.no_warm or world > 1) else measure_warm_start()
+    f64 = None
+    if world == 1 and args.ntraj == NTRAJ and not args.no_f64:
+        f64 = measure_f64(twmc, torch)
+        f64["fp32_speedup"] = value / f64["value"]
     hbm = peaks.get("hbm_gbs")
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -353,7 +380,7 @@ def main():
                              "peak_gbs": hbm, "source": "MEASURED_PEAKS.json" if hbm else None}},
         "issue": issue, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu, "clocks": clocks,
         "trajectories_per_s": value / (NX * NY * (T_END / DT)), "finite": finite,
-        "kernel_ms": kernel_ms, "time_to_steady_state": warm,
+        "kernel_ms": kernel_ms, "time_to_steady_state": warm, "fp64_mode": f64,
     }
     print(json.dumps(line), flush=True)
     if dist:

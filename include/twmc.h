@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define TWMC_ABI_VERSION 1
+#define TWMC_ABI_VERSION 2
 
 #if defined(__GNUC__)
 #define TWMC_API __attribute__((visibility("default")))
@@ -111,6 +111,13 @@ typedef struct twmc_system_desc {
   int32_t noise_mode;  /* twmc_noise_mode */
   int32_t hop_mode;    /* twmc_hop_mode (square lattice) */
   int32_t n_moment_blocks; /* ensemble blocks for standard errors (0 = 32) */
+  /* Square lattice: accumulate the drive's work and area per site between
+   * saves (TWMCThermoSolver.cpp:203-236, the solver the reference's manager
+   * selects for a periodic lattice with F(t), TWMCManager.cpp:47-58):
+   *   work += 2 dt Re(b) dF/dt,  area += dt dF/dt (|b|^2 - 1/2),
+   *   dF/dt = Re(F(t) - F(t - dt)) / dt (0 on a run's first step),
+   * b the field after the step. Runs on the real-space kernel. */
+  int32_t thermo;
 } twmc_system_desc;
 
 typedef struct twmc_task_desc {
@@ -136,6 +143,9 @@ typedef struct twmc_outputs {
   int64_t* frames_written; /* optional: n_tasks (frames actually produced) */
   double* t_final;         /* optional: n_tasks (extraDataMemory[1]) */
   int32_t* status;         /* optional: n_tasks (0 or TWMC_ERR_NONFINITE) */
+  double* work;            /* optional (thermo): n_tasks x n_frames x n_sites float64 ("work" dataset),
+                              accumulated since the previous saved frame (0 for an initial frame) */
+  double* area;            /* optional (thermo): same layout ("area" dataset) */
 } twmc_outputs;
 
 typedef struct twmc_handle twmc_handle;

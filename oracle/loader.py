@@ -26,6 +26,10 @@ def _setup(lib):
                                  C.c_double, C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_void_p, C.c_void_p,
                                  C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
                                  C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
+    lib.orc_thermo_run.argtypes = [C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double,
+                                   C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p,
+                                   C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_uint32,
+                                   C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.orc_time_table_eval.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int64,
                                         C.c_void_p]
     lib.orc_initial_field.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
@@ -94,6 +98,35 @@ def base_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, store_
                             meta.ctypes.data)
     return {"frames": frames[: int(meta[0])], "final": beta, "frames_written": int(meta[0]), "t_final": meta[1],
             "steps": int(meta[2])}
+
+
+def thermo_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, store_initial, omega, U, F, beta0,
+               F_t=None, xi=None, seed=0, tid=0, noise="buffer"):
+    """Square lattice with an F(t) table and the drive's work / area datasets."""
+    n = nx * ny
+    om, u, f = (_c(np.broadcast_to(v, (n,))) for v in (omega, U, F))
+    beta = _c(beta0).copy()
+    nf = max(n_frames, 1)
+    frames = np.zeros((nf, n), dtype=np.complex128)
+    work = np.zeros((nf, n))
+    area = np.zeros((nf, n))
+    meta = np.zeros(3)
+    xi_c = _c(xi) if xi is not None else None
+    if F_t is not None:
+        ft_t = np.ascontiguousarray(np.asarray(F_t[0], dtype=np.float64))
+        ft_v = _c(F_t[1])
+        nrec = len(ft_t)
+    else:
+        ft_t = ft_v = None
+        nrec = 0
+    load().orc_thermo_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, int(store_initial),
+                          om.ctypes.data, u.ctypes.data, f.ctypes.data, nrec,
+                          None if ft_t is None else ft_t.ctypes.data, None if ft_v is None else ft_v.ctypes.data,
+                          beta.ctypes.data, NOISE[noise], None if xi_c is None else xi_c.ctypes.data, seed, tid,
+                          frames.ctypes.data, work.ctypes.data, area.ctypes.data, meta.ctypes.data)
+    k = int(meta[0])
+    return {"frames": frames[:k], "work": work[:k], "area": area[:k], "final": beta, "frames_written": k,
+            "t_final": meta[1], "steps": int(meta[2])}
 
 
 def lieb_run(ncell, pbc, J_AB, J_BC, detuning, gamma, dt, t_start, t_end, frame_steps, n_frames, store_initial,

@@ -309,24 +309,17 @@ void orc_frame_grid(double t_start, double t_end, double timestep, double frames
   out[4] = double(nf);
 }
 
-// One trajectory of TWMCBaseSolver::Compute's hot loop (TWMCBaseSolver.cpp:206-280)
-// on an nx x ny lattice (row-major, after the 1-D swap of TWMCSystemData).
-//   omega, U, F      per-site complex (interleaved), nx*ny each
-//   beta             in: initial field; out: field at the end
-//   noise_mode       0 = buffer xi[step][site] (interleaved complex normals)
-//                    1 = Philox FP64 flavour, 2 = Philox FP32 flavour
-//   frames           out: n_frames * nx*ny complex (may be NULL)
-//   out_meta         [frames_written, t_final, steps_run]
-// Returns 0.
-int orc_base_run(int64_t nx, int64_t ny, double J, double gamma, double dt, double t_start, double t_end,
-                 int64_t frame_steps, int64_t n_frames, int store_initial, const double* omega_ri,
-                 const double* U_ri, const double* F_ri, double* beta_ri, int noise_mode, const double* xi_ri,
-                 uint32_t seed, uint32_t tid, double* frames_ri, double* out_meta) {
+// Square-lattice loop shared by the base and thermo runs (below).
+static int square_run(int64_t nx, int64_t ny, double J, double gamma, double dt, double t_start, double t_end,
+                      int64_t frame_steps, int64_t n_frames, int store_initial, const double* omega_ri,
+                      const double* U_ri, const double* F_ri, int64_t ft_nrec, const double* ft_times,
+                      const double* ft_vals_ri, double* beta_ri, int noise_mode, const double* xi_ri, uint32_t seed,
+                      uint32_t tid, double* frames_ri, double* work, double* area, double* out_meta) {
   const int64_t n = nx * ny;
   cd* beta = reinterpret_cast<cd*>(beta_ri);
   const cd* omega = reinterpret_cast<const cd*>(omega_ri);
   const cd* U = reinterpret_cast<const cd*>(U_ri);
-  const cd* F = reinterpret_cast<const cd*>(F_ri);
+  std::vector<cd> F(reinterpret_cast<const cd*>(F_ri), reinterpret_cast<const cd*>(F_ri) + n);
   const cd ij(0.0, 1.0);
   // Setup (:65-91)
   std::vector<cd> rsl(static_cast<size_t>(n)), kstep(static_cast<size_t>(n));
@@ -340,14 +333,29 @@ int orc_base_run(int64_t nx, int64_t ny, double J, double gamma, double dt, doub
   const double norm = double(n);
   const double dt4 = std::sqrt(gamma * dt / 4.0);
   std::vector<cd> fin(static_cast<size_t>(n)), a(static_cast<size_t>(n)), xi(static_cast<size_t>(n));
+  TimeTable tt;
+  const bool timedep = ft_nrec > 0;
+  if (timedep) tt = build_time_table(ft_times, ft_vals_ri, ft_nrec, n);
+  int64_t tcache = 0;
+  const bool thermo = work != nullptr;
+  std::vector<cd> Fprev(static_cast<size_t>(n));
+  std::vector<double> dW(static_cast<size_t>(n), 0.0), dA(static_cast<size_t>(n), 0.0);
   int64_t i_step = 0, i_frame = 0;
   if (store_initial && n_frames > 0) {
     if (frames_ri) std::memcpy(frames_ri, beta, sizeof(cd) * size_t(n));
+    if (thermo) {
+      std::fill(work, work + n, 0.0);
+      std::fill(area, area + n, 0.0);
+    }
     i_frame = 1;
   }
   double t = t_start;
   cd* frames = reinterpret_cast<cd*>(frames_ri);
   while (t <= t_end) {
+    if (timedep) {
+      tcache = time_table_eval(tt, t, tcache, F.data());
+      if (i_step == 0) Fprev = F;  // dF/dt is 0 on a run's first step
+    }
     fin.assign(beta, beta + n);
     fft2d(fin.data(), nx, ny, -1);
     for (int64_t i = 0; i < n; ++i) fin[size_t(i)] = kstep[size_t(i)] * fin[size_t(i)];
@@ -355,7 +363,7 @@ int orc_base_run(int64_t nx, int64_t ny, double J, double gamma, double dt, doub
     for (int64_t i = 0; i < n; ++i) fin[size_t(i)] = fin[size_t(i)] / norm;
     for (int64_t i = 0; i < n; ++i) {
       const double ab2 = beta[i].real() * beta[i].real() + beta[i].imag() * beta[i].imag();
-      a[size_t(i)] = ((rsl[size_t(i)] + ij * U[i] * (ab2 - 1.0)) * beta[i] + fin[size_t(i)] + ij * F[i]) * dt;
+      a[size_t(i)] = ((rsl[size_t(i)] + ij * U[i] * (ab2 - 1.0)) * beta[i] + fin[size_t(i)] + ij * F[size_t(i)]) * dt;
     }
     if (noise_mode == 0) {
       const cd* src = reinterpret_cast<const cd*>(xi_ri) + i_step * n;
@@ -365,10 +373,25 @@ int orc_base_run(int64_t nx, int64_t ny, double J, double gamma, double dt, doub
         xi[size_t(i)] = site_normal(seed, tid, uint32_t(i_step), kStreamWiener, i, n, noise_mode == 2);
     }
     for (int64_t i = 0; i < n; ++i) beta[i] = beta[i] + a[size_t(i)] + dt4 * xi[size_t(i)];
+    if (thermo) {  // TWMCThermoSolver.cpp:230-236 with dF/dt from consecutive steps
+      for (int64_t i = 0; i < n; ++i) {
+        const double fd = timedep ? (F[size_t(i)].real() - Fprev[size_t(i)].real()) / dt : 0.0;
+        const double x = beta[i].real();
+        dW[size_t(i)] += (2.0 * dt) * x * fd;
+        dA[size_t(i)] += (dt * fd) * (std::norm(beta[i]) - 0.5);
+      }
+      if (timedep) Fprev = F;
+    }
     t += dt;
     ++i_step;
     if ((i_step % frame_steps == 0) && i_frame < n_frames) {
       if (frames) std::memcpy(frames + i_frame * n, beta, sizeof(cd) * size_t(n));
+      if (thermo) {
+        std::memcpy(work + i_frame * n, dW.data(), sizeof(double) * size_t(n));
+        std::memcpy(area + i_frame * n, dA.data(), sizeof(double) * size_t(n));
+        std::fill(dW.begin(), dW.end(), 0.0);
+        std::fill(dA.begin(), dA.end(), 0.0);
+      }
       ++i_frame;
       if (i_frame == n_frames) break;
     }
@@ -377,6 +400,41 @@ int orc_base_run(int64_t nx, int64_t ny, double J, double gamma, double dt, doub
   out_meta[1] = t;
   out_meta[2] = double(i_step);
   return 0;
+}
+
+// One trajectory of TWMCBaseSolver::Compute's hot loop (TWMCBaseSolver.cpp:206-280)
+// on an nx x ny lattice (row-major, after the 1-D swap of TWMCSystemData).
+//   omega, U, F      per-site complex (interleaved), nx*ny each
+//   beta             in: initial field; out: field at the end
+//   noise_mode       0 = buffer xi[step][site] (interleaved complex normals)
+//                    1 = Philox FP64 flavour, 2 = Philox FP32 flavour
+//   frames           out: n_frames * nx*ny complex (may be NULL)
+//   out_meta         [frames_written, t_final, steps_run]
+// Returns 0.
+int orc_base_run(int64_t nx, int64_t ny, double J, double gamma, double dt, double t_start, double t_end,
+                 int64_t frame_steps, int64_t n_frames, int store_initial, const double* omega_ri,
+                 const double* U_ri, const double* F_ri, double* beta_ri, int noise_mode, const double* xi_ri,
+                 uint32_t seed, uint32_t tid, double* frames_ri, double* out_meta) {
+  return square_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, store_initial, omega_ri, U_ri, F_ri,
+                    0, nullptr, nullptr, beta_ri, noise_mode, xi_ri, seed, tid, frames_ri, nullptr, nullptr, out_meta);
+}
+
+// The square-lattice loop with an F(t) table (evaluated at the pre-step t, as
+// NoisyMatrix::GetAtTimeWithSuggestion in TWMCThermoSolver.cpp:206-210) and
+// the drive's work and area per site (TWMCThermoSolver.cpp:230-236):
+//   work += 2 dt Re(b) dF/dt,  area += dt dF/dt (|b|^2 - 1/2)
+// with b the field after the step and dF/dt = Re(F(t) - F(t - dt)) / dt (0 on
+// the first step), summed between saved frames and reset at each save (an
+// initial frame has 0). work, area: out, n_frames * nx*ny doubles each.
+int orc_thermo_run(int64_t nx, int64_t ny, double J, double gamma, double dt, double t_start, double t_end,
+                   int64_t frame_steps, int64_t n_frames, int store_initial, const double* omega_ri,
+                   const double* U_ri, const double* F_ri, int64_t ft_nrec, const double* ft_times,
+                   const double* ft_vals_ri, double* beta_ri, int noise_mode, const double* xi_ri, uint32_t seed,
+                   uint32_t tid, double* frames_ri, double* work, double* area, double* out_meta) {
+  if (!work || !area) return -1;
+  return square_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, store_initial, omega_ri, U_ri, F_ri,
+                    ft_nrec, ft_times, ft_vals_ri, beta_ri, noise_mode, xi_ri, seed, tid, frames_ri, work, area,
+                    out_meta);
 }
 
 // One trajectory of TWMCLiebSolver::Compute's hot loop (TWMCLiebSolver.cpp:222-294)

@@ -92,6 +92,8 @@ struct twmc_handle {
   Matrix m_omega, m_U, m_F, m_binit, m_bsigma;
   // F(t)
   bool timedep = false;
+  bool thermo = false;     // work / area accumulators (TWMCThermoSolver)
+  DevBuf d_work, d_area;
   std::vector<double> ft_times;   // with sentinel
   std::vector<cd> ft_vals, ft_slopes;
   // kernel selection
@@ -416,6 +418,10 @@ int advance(twmc_handle* h, int64_t n, bool want_nk) {
     a.ft_id = h->d_ft_id.as<int>();
     a.ft_dt = h->d_ft_dt.as<double>();
   }
+  if (h->thermo) {
+    a.work = h->d_work.p;
+    a.area = h->d_area.p;
+  }
   if (h->noise_mode == TWMC_NOISE_BUFFER && n > 0 && int64_t(h->step_pos) + n > h->noise_steps)
     return fail(h, TWMC_ERR_INVALID, "noise buffer shorter than the run");
   int nparams = 0;
@@ -465,6 +471,12 @@ int batch_init(twmc_handle* h, const twmc_task_desc* tasks, size_t n) {
   if (!h->d_moments.ensure(size_t(h->nblocks) * N * 3 * sizeof(double))) return fail(h, TWMC_ERR_NOMEM, "moments allocation");
   if (!h->d_status.ensure(n * sizeof(int))) return fail(h, TWMC_ERR_NOMEM, "status allocation");
   TWMC_CUDA(h, cudaMemsetAsync(h->d_status.p, 0, n * sizeof(int), h->stream));
+  if (h->thermo) {
+    if (!h->d_work.ensure(n * N * rsize(prec)) || !h->d_area.ensure(n * N * rsize(prec)))
+      return fail(h, TWMC_ERR_NOMEM, "work / area allocation");
+    TWMC_CUDA(h, cudaMemsetAsync(h->d_work.p, 0, n * N * rsize(prec), h->stream));
+    TWMC_CUDA(h, cudaMemsetAsync(h->d_area.p, 0, n * N * rsize(prec), h->stream));
+  }
   std::vector<uint32_t> seeds(n), ids(n);
   int ic = tasks[0].ic_kind;
   for (size_t i = 0; i < n; ++i) {
@@ -543,6 +555,19 @@ int batch_init(twmc_handle* h, const twmc_task_desc* tasks, size_t n) {
   return TWMC_OK;
 }
 
+// Copies n real values (state precision) of a device buffer to host doubles.
+int download_real(twmc_handle* h, const DevBuf& b, double* out, size_t n) {
+  TWMC_CUDA(h, cudaStreamSynchronize(h->stream));
+  if (h->prec == 0) {
+    std::vector<float> tmp(n);
+    TWMC_CUDA(h, cudaMemcpy(tmp.data(), b.p, n * sizeof(float), cudaMemcpyDeviceToHost));
+    for (size_t i = 0; i < n; ++i) out[i] = double(tmp[i]);
+  } else {
+    TWMC_CUDA(h, cudaMemcpy(out, b.p, n * sizeof(double), cudaMemcpyDeviceToHost));
+  }
+  return TWMC_OK;
+}
+
 int download_field(twmc_handle* h, double* out) {
   const size_t n = size_t(h->ntraj * h->nsites);
   if (h->prec) {
@@ -577,6 +602,10 @@ int validate_desc(const twmc_system_desc* d, std::string* why) {
   }
   if (d->beta_init.noise_kind != 0 || d->beta_init_sigma.noise_kind != 0) {
     *why = "noise on beta_init / beta_init_sigma is not supported";
+    return TWMC_ERR_INVALID;
+  }
+  if (d->thermo != 0 && d->lattice != TWMC_LATTICE_SQUARE) {
+    *why = "work / area accumulation is defined for the square lattice only";
     return TWMC_ERR_INVALID;
   }
   if (d->ft_nrec > 0) {
@@ -626,8 +655,9 @@ int twmc_create(const twmc_system_desc* d, twmc_handle** out) {
       h->timedep = true;
       build_time_table(h, d->ft_times, d->ft_values, d->ft_nrec);
     }
+    h->thermo = d->thermo != 0;
     setup_params(h);
-    if (h->lattice == TWMC_LATTICE_SQUARE && h->hop_mode == TWMC_HOP_FFT && !h->timedep) {
+    if (h->lattice == TWMC_LATTICE_SQUARE && h->hop_mode == TWMC_HOP_FFT && !h->timedep && !h->thermo) {
       const int bx = ilog2_exact(h->nx), by = ilog2_exact(h->ny);
       PlanView pv;
       if (bx >= 0 && by >= 0 && square_plan(bx, by, &pv)) { h->use_fft = true; h->bx = bx; h->by = by; }
@@ -826,6 +856,20 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
           if (r2) return r2;
           for (size_t i = 0; i < bn; ++i)
             std::memcpy(out->frames + (idx[i] * max_frames + f) * N * 2, &fbuf[i * N * 2], sizeof(double) * size_t(N * 2));
+        }
+        if (h->thermo) {  // work / area since the previous save, then reset
+          double* dst[2] = {out ? out->work : nullptr, out ? out->area : nullptr};
+          DevBuf* src[2] = {&h->d_work, &h->d_area};
+          for (int k = 0; k < 2; ++k) {
+            if (dst[k]) {
+              std::vector<double> v(size_t(bn * N));
+              int r2 = download_real(h, *src[k], v.data(), size_t(bn * N));
+              if (r2) return r2;
+              for (size_t i = 0; i < bn; ++i)
+                std::memcpy(dst[k] + (idx[i] * max_frames + f) * N, &v[i * N], sizeof(double) * size_t(N));
+            }
+            TWMC_CUDA(h, cudaMemsetAsync(src[k]->p, 0, size_t(bn * N) * rsize(h->prec), h->stream));
+          }
         }
         return TWMC_OK;
       };

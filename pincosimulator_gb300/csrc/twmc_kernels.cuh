@@ -63,6 +63,11 @@ struct StepArgs {
   const int* ft_id;       // [total steps] segment id per step
   const double* ft_dt;    // [total steps] t - t_id per step
   int dbuf;               // ell: double-buffered exchange
+  // drive thermodynamics (ell kernel, TWMCThermoSolver.cpp:203-236): per-site
+  // accumulators [ntraj][N] (R) of work 2 dt Re(beta) dF/dt and area
+  // dt dF/dt (|beta|^2 - 1/2), dF/dt = Re(F(t) - F(t - dt)) / dt; NULL = off
+  void* work;
+  void* area;
 };
 
 __device__ __forceinline__ void set_status(int* status, int64_t traj, bool bad) {
@@ -588,11 +593,14 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
           return cmake<T>(J * s.y, -J * s.x);  // -i J s
         }
       };
-      int id_t = 0;
-      R dtt = R(0);
+      int id_t = 0, id_p = 0;
+      R dtt = R(0), dtp = R(0), seg_ratio = R(0);
       if (timedep) {
         id_t = a.ft_id[gstep];
         dtt = R(a.ft_dt[gstep]);
+        id_p = gstep > 0 ? a.ft_id[gstep - 1] : id_t;
+        dtp = gstep > 0 ? R(a.ft_dt[gstep - 1]) : dtt;
+        if (a.work != nullptr && gstep > 0) seg_ratio = R((a.ft_dt[gstep] - a.ft_dt[gstep - 1]) / a.dt);
       }
 #pragma unroll
       for (int v = 0; v < H; ++v) {
@@ -619,6 +627,25 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
             f = cmake<T>(f0.x + dtt * f1.x, f0.y + dtt * f1.y);
           }
           beta[vv] = local_update(beta[vv], hop(vv), r, u, f, dt, dt4, q ? xi_hi : xi_lo);
+          if (a.work != nullptr && valid[vv] && active) {
+            R fd = R(0);
+            if (timedep && gstep > 0) {  // Re F = Im(i F); the first step of a run has F(t - dt) = F(t)
+              if (id_p == id_t) {
+                // same table segment: the difference is the slope times the
+                // time step, free of the cancellation of F(t) - F(t - dt)
+                fd = __ldg(reinterpret_cast<const T*>(a.ft_slopes) + int64_t(id_t) * N + p).y * seg_ratio;
+              } else {
+                const T g0 = __ldg(reinterpret_cast<const T*>(a.ft_vals) + int64_t(id_p) * N + p);
+                const T g1 = __ldg(reinterpret_cast<const T*>(a.ft_slopes) + int64_t(id_p) * N + p);
+                fd = (f.y - (g0.y + dtp * g1.y)) / dt;
+              }
+            }
+            const T b = beta[vv];
+            R* wk = reinterpret_cast<R*>(a.work) + tr * N + p;
+            R* ar = reinterpret_cast<R*>(a.area) + tr * N + p;
+            *wk += (R(2) * dt) * b.x * fd;
+            *ar += (dt * fd) * (b.x * b.x + b.y * b.y - R(0.5));
+          }
         }
       }
       if (a.dbuf) buf ^= 1; else __syncthreads();

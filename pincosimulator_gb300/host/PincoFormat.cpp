@@ -158,9 +158,11 @@ void PincoArchive::Store(const TWMCResults& r) {
     const size_t j = size_t(it - names_.begin());
     FILE* f = c->files[j];
     const long start = std::ftell(f);
-    const size_t bytes = d.data.size() * sizeof(cplx);
+    const bool real = formats_[j] == 11;
+    const size_t bytes = real ? d.rdata.size() * sizeof(double) : d.data.size() * sizeof(cplx);
     std::fwrite(&bytes, sizeof(size_t), 1, f);
-    std::fwrite(d.data.data(), 1, bytes, f);
+    if (real) std::fwrite(d.rdata.data(), 1, bytes, f);
+    else std::fwrite(d.data.data(), 1, bytes, f);
     std::fflush(f);
     const long end = std::ftell(f);
     c->total += size_t(end - start + 1);  // the reference's size accounting
@@ -229,8 +231,12 @@ std::unique_ptr<TWMCResults> PincoArchive::Load(size_t id, bool last_frame_only)
         bytes = el;
         nel = 1;
       }
-      std::vector<cplx> data(bytes / sizeof(cplx));
-      const size_t rb = bytes ? std::fread(data.data(), 1, bytes, fc) : 0;
+      const bool real = formats_[j] == 11;
+      std::vector<cplx> data(real ? 0 : bytes / sizeof(cplx));
+      std::vector<double> rdata(real ? bytes / sizeof(double) : 0);
+      const size_t rb = bytes ? std::fread(real ? static_cast<void*>(rdata.data()) : static_cast<void*>(data.data()),
+                                           1, bytes, fc)
+                              : 0;
       std::fclose(fc);
       if (rb != bytes) fail("truncated chunk record in " + cp);
       Dataset* dst = nullptr;
@@ -244,11 +250,14 @@ std::unique_ptr<TWMCResults> PincoArchive::Load(size_t id, bool last_frame_only)
         res->datasets.push_back(d);
         dst = &res->datasets.back();
       }
-      if (names_[j] == "traj") {  // trajectories append, realisations are replaced
+      const bool series = names_[j] == "traj" || names_[j] == "work" || names_[j] == "area";
+      if (series) {  // frame series append across continuations, realisations are replaced
         dst->data.insert(dst->data.end(), data.begin(), data.end());
+        dst->rdata.insert(dst->rdata.end(), rdata.begin(), rdata.end());
         dst->frames += nel;
       } else {
         dst->data = data;
+        dst->rdata = rdata;
         dst->frames = nel;
       }
     }

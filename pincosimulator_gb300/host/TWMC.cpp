@@ -214,6 +214,10 @@ void TWMCCudaSolver::SetupFor(const TWMCSystemData* d) {
   desc.precision = d->precision == "f64" ? TWMC_PREC_F64 : TWMC_PREC_F32;
   desc.noise_mode = TWMC_NOISE_PHILOX;
   desc.hop_mode = d->hop == "stencil" ? TWMC_HOP_STENCIL : TWMC_HOP_FFT;
+  // the reference's manager runs a periodic lattice with F(t) on its Thermo
+  // solver, which adds the work and area datasets (TWMCManager.cpp:47-58)
+  thermo_ = !lieb && d->F.HasTimeDependence();
+  desc.thermo = thermo_ ? 1 : 0;
   const int rc = twmc_create(&desc, &h_);
   if (rc != TWMC_OK) {
     err_ = std::string("twmc_create failed: ") + (h_ ? twmc_last_error(h_) : "");
@@ -261,9 +265,14 @@ std::vector<std::unique_ptr<TaskResults>> TWMCCudaSolver::Compute(const std::vec
     std::vector<int64_t> fw(n);
     std::vector<double> tf(n);
     std::vector<int32_t> st(n);
+    std::vector<double> work(thermo_ ? frames.size() : 0), area(thermo_ ? frames.size() : 0);
     twmc_outputs o;
     std::memset(&o, 0, sizeof(o));
     o.frames = reinterpret_cast<double*>(frames.data());
+    if (thermo_) {
+      o.work = work.data();
+      o.area = area.data();
+    }
     o.U_realization = reinterpret_cast<double*>(ru.data());
     o.omega_realization = reinterpret_cast<double*>(ro.data());
     o.F_realization = reinterpret_cast<double*>(rf.data());
@@ -300,6 +309,18 @@ std::vector<std::unique_ptr<TaskResults>> TWMCCudaSolver::Compute(const std::vec
       traj.dims = dims;
       traj.data.assign(frames.begin() + long(k * max_frames * N), frames.begin() + long((k * max_frames + size_t(fw[k])) * N));
       r->datasets.push_back(std::move(traj));
+      if (thermo_) {  // TWMCThermoSolver.cpp:280-282: traj, work, area
+        for (int q = 0; q < 2; ++q) {
+          const std::vector<double>& src = q ? area : work;
+          Dataset ds;
+          ds.name = q ? "area" : "work";
+          ds.format = 11;
+          ds.frames = size_t(fw[k]);
+          ds.dims = dims;
+          ds.rdata.assign(src.begin() + long(k * max_frames * N), src.begin() + long((k * max_frames + size_t(fw[k])) * N));
+          r->datasets.push_back(std::move(ds));
+        }
+      }
       r->extra[0] = t->t_start;
       r->extra[1] = tf[k];
       r->status = st[k];

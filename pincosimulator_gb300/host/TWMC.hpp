@@ -69,7 +69,8 @@ struct Dataset {
   unsigned char format = 22;  // 22 = complex128, 11 = float64
   size_t frames = 1;          // elements in the frames dimension
   std::vector<size_t> dims;   // {nx, ny} or {nx, ny, 3}
-  std::vector<cplx> data;
+  std::vector<cplx> data;     // format 22
+  std::vector<double> rdata;  // format 11
 };
 
 class TWMCResults : public TaskResults {
@@ -95,6 +96,7 @@ class TWMCCudaSolver : public Solver {
   void SetupFor(const TWMCSystemData* data);
   const TWMCSystemData* last_ = nullptr;
   twmc_handle* h_ = nullptr;
+  bool thermo_ = false;  // work / area datasets (F(t) on a periodic lattice)
   std::string err_;
   std::vector<double> ft_times_, ft_vals_;
 };

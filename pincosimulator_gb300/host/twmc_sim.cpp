@@ -70,6 +70,38 @@ void describe(const Settings& s, const TWMCSystemData& d) {
   std::cout << o.str() << std::endl;
 }
 
+// The merge manager (MergeManager.cpp:54-102, registered as "merge"): every
+// trajectory of oldArchive1, then of oldArchive2, is loaded whole
+// (continuations joined) and stored in the archive under the output folder.
+// An id present in both archives is stored twice, the second time as a
+// continuation of the first, as the reference's saver does. The save-time
+// tables (_t.dat, _F_t.dat) of the first archive are copied when present.
+int merge(const Settings& s) {
+  const fs::path out = fs::path(s.GetOutputFolder()) / "data";
+  fs::create_directories(out);
+  PincoArchive dst(out.string(), s.getDouble("chunk_size", 1.5));
+  size_t n = 0;
+  for (const char* key : {"oldArchive1", "oldArchive2"}) {
+    const std::string root = s.getString(key);
+    if (root.empty()) throw std::runtime_error(std::string("merge: missing key ") + key);
+    const fs::path src = fs::path(root) / "data";
+    if (!fs::exists(src / "_register.bin")) throw std::runtime_error("merge: no archive in " + src.string());
+    PincoArchive a(src.string());
+    std::cout << "Loading data from: " << root << " (" << a.UsedIds().size() << " trajectories)" << std::endl;
+    for (size_t id : a.UsedIds()) {
+      auto r = a.Load(id, false);
+      if (!r) throw std::runtime_error("merge: cannot load trajectory " + std::to_string(id));
+      dst.Store(*r);
+      ++n;
+    }
+    if (std::string(key) == "oldArchive1")
+      for (const char* f : {"_t.dat", "_F_t.dat"})
+        if (fs::exists(src / f) && !fs::exists(out / f)) fs::copy_file(src / f, out / f);
+  }
+  std::cout << "Saved " << n << " items." << std::endl;
+  return 0;
+}
+
 }  // namespace
 
 int main(int argc, char** argv) {
@@ -81,6 +113,7 @@ int main(int argc, char** argv) {
   }
   try {
     Settings settings(int(args.size()), args.data());
+    if (settings.getString("Manager") == "merge") return merge(settings);
     auto sys = std::make_shared<TWMCSystemData>(settings);
     if (want_describe) {
       describe(settings, *sys);

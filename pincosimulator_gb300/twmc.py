@@ -52,6 +52,7 @@ class SystemDesc(C.Structure):
         ("omega", Matrix), ("U", Matrix), ("F", Matrix), ("beta_init", Matrix), ("beta_init_sigma", Matrix),
         ("ft_nrec", C.c_int64), ("ft_times", C.c_void_p), ("ft_values", C.c_void_p),
         ("precision", C.c_int32), ("noise_mode", C.c_int32), ("hop_mode", C.c_int32), ("n_moment_blocks", C.c_int32),
+        ("thermo", C.c_int32),
     ]
 
 
@@ -77,6 +78,7 @@ class Outputs(C.Structure):
         ("frames", C.c_void_p), ("final_field", C.c_void_p), ("U_realization", C.c_void_p),
         ("omega_realization", C.c_void_p), ("F_realization", C.c_void_p), ("moments", C.c_void_p),
         ("frames_written", C.c_void_p), ("t_final", C.c_void_p), ("status", C.c_void_p),
+        ("work", C.c_void_p), ("area", C.c_void_p),
     ]
 
 
@@ -194,7 +196,8 @@ class System:
 
     def __init__(self, *, lattice=LATTICE_SQUARE, nx=1, ny=1, pbc=True, J=0.0, J_AB=0.0, J_BC=0.0, gamma=1.0,
                  detuning=0.0, dt=0.01, frame_steps=1, omega=0.0, U=0.0, F=0.0, beta_init=0.0, beta_init_sigma=0.0,
-                 F_t: Optional[tuple] = None, precision=PREC_F32, noise=NOISE_PHILOX, hop=HOP_FFT, n_moment_blocks=32):
+                 F_t: Optional[tuple] = None, precision=PREC_F32, noise=NOISE_PHILOX, hop=HOP_FFT, n_moment_blocks=32,
+                 thermo=False):
         self.lib = load()
         self.n_sites = (3 if lattice == LATTICE_LIEB else 1) * nx * ny
         n = self.n_sites
@@ -217,6 +220,8 @@ class System:
             self._keep += [times, vals]
             d.ft_nrec, d.ft_times, d.ft_values = len(times), times.ctypes.data, vals.ctypes.data
         d.precision, d.noise_mode, d.hop_mode, d.n_moment_blocks = precision, noise, hop, n_moment_blocks
+        d.thermo = int(bool(thermo))
+        self.thermo = bool(thermo)
         self.desc = d
         self.n_blocks = n_moment_blocks
         self.precision = precision
@@ -309,6 +314,10 @@ class System:
         if realizations:
             for key in ("U_realization", "omega_realization", "F_realization"):
                 res[key] = np.zeros((n, N), dtype=np.complex128)
+                setattr(out, key, res[key].ctypes.data)
+        if self.thermo and frames:
+            for key in ("work", "area"):
+                res[key] = np.zeros((n, n_frames, N), dtype=np.float64)
                 setattr(out, key, res[key].ctypes.data)
         res["frames_written"] = np.zeros(n, dtype=np.int64)
         res["t_final"] = np.zeros(n, dtype=np.float64)

@@ -58,23 +58,30 @@ def read_entry(data_dir, reg, entry):
         with open(os.path.join(data_dir, f"variable{j}_{entry['chunk']}.cnk"), "rb") as f:
             f.seek(off)
             (nbytes,) = struct.unpack("<Q", f.read(8))
-            data = np.frombuffer(f.read(nbytes), dtype=np.complex128)
+            dtype = np.float64 if reg["formats"][j] == 11 else np.complex128
+            data = np.frombuffer(f.read(nbytes), dtype=dtype)
         out[name] = (nel, data)
     return out
 
 
 def read_trajectory(data_dir, traj_id):
-    """All entries of one trajectory in register order; traj frames concatenated."""
+    """All entries of one trajectory in register order: (traj frames
+    concatenated, the other datasets of the last entry, entries); the frame
+    series work / area (float64) are concatenated into the second result."""
     reg = read_register(data_dir)
     ents = [e for e in reg["entries"] if e["id"] == traj_id]
-    frames, real = [], {}
+    frames, real, series = [], {}, {}
     for e in ents:
         d = read_entry(data_dir, reg, e)
         for name, (nel, data) in d.items():
             if name == "traj":
                 frames.append(data.reshape(nel, -1))
+            elif name in ("work", "area"):
+                series.setdefault(name, []).append(data.reshape(nel, -1))
             else:
                 real[name] = data
+    for name, parts in series.items():
+        real[name] = np.concatenate(parts)
     return (np.concatenate(frames) if frames else None), real, ents
 
 

@@ -140,3 +140,57 @@ def test_lieb_ini_runs(sim, tmp_path):
     assert reg["names"] == ["Omega_Realization", "traj"] and reg["dims"][1] == [1, 24, 3]
     fr, real, _ = pr.read_trajectory(out / "data", 1)
     assert fr.shape == (3, 72) and np.isfinite(fr).all()
+
+
+def test_time_dependent_drive_writes_work_and_area(sim, tmp_path):
+    """A periodic lattice with F(t) runs in thermo mode (the reference's
+    manager picks its Thermo solver there): the archive gains the float64
+    datasets work and area after traj, equal to the same run through the C
+    ABI (the time table read at float precision, as the reader does)."""
+    times = [0.0, 0.5, 1.0]
+    amp = [0.0, 2.0, 2.0]
+    lines = []
+    for t, a in zip(times, amp):
+        lines.append(f"{t}")
+        for r in range(4):
+            lines.append("  ".join(f"{a * (1 + 0.1 * (r * 4 + c)):.6f}" for c in range(4)))
+        lines.append("")
+    (tmp_path / "F_t.dat").write_text("\n".join(lines) + "\n")
+    ini = tmp_path / "thermo.ini"
+    ini.write_text("""
+Manager = "TWMC"
+nx = 4
+ny = 4
+PBC = true
+J = 1
+U = 0.2
+gamma = 1
+omega = -0.5
+F_t = "F_t.dat"
+beta_init = 0
+beta_init_sigma = 0.5
+timestep = 0.01
+t_start = 0
+t_end = 1.5
+frames_period = 0.5
+n_traj = 3
+SEED = 9
+""")
+    out = tmp_path / "out"
+    run_sim(sim, ini, out)
+    data = out / "data"
+    reg = pr.read_register(data)
+    assert reg["names"] == ["traj", "work", "area"] and reg["formats"] == [22, 11, 11]
+    seeds = mt19937(9, 3)
+    vals = np.array([[np.float32(a * (1 + 0.1 * k)) for k in range(16)] for a in amp], dtype=np.float64)
+    s = twmc.System(nx=4, ny=4, J=1.0, gamma=1.0, dt=0.01, frame_steps=50, omega=-0.5, U=0.2, F=0.0,
+                    beta_init_sigma=0.5, F_t=(np.array(times), vals.astype(complex)), thermo=True)
+    tasks = s.make_tasks(3, t_start=0.0, t_end=1.5, seeds=seeds, id0=1)
+    res = s.run(tasks, frames=True)
+    s.close()
+    for k in range(3):
+        fr, real, _ = pr.read_trajectory(data, k + 1)
+        assert fr.shape == (4, 16) and np.array_equal(fr, res["frames"][k])
+        assert real["work"].shape == (4, 16) and np.array_equal(real["work"], res["work"][k])
+        assert np.array_equal(real["area"], res["area"][k])
+        assert np.all(real["work"][0] == 0) and np.abs(real["work"][1]).max() > 0

@@ -9,7 +9,7 @@ import pytest
 
 from pincosimulator_gb300 import twmc
 
-from gpu_util import check, lieb_case, square_case
+from gpu_util import check, lieb_case, rel_err, square_case
 
 pytestmark = pytest.mark.gpu
 
@@ -74,3 +74,41 @@ def test_lieb_time_dependent_drive(built_lib, oracle, prec):
     vals[:, 1::3] = (2.5 * times / 0.25)[:, None]
     res, refs = lieb_case(oracle, ncell, prec=prec, steps=200, dt=0.002, F_t=(times, vals))
     check(res, refs, prec)
+
+
+@pytest.mark.parametrize("prec", [twmc.PREC_F32, twmc.PREC_F64])
+@pytest.mark.parametrize("shape", [(8, 8), (1, 48)])
+def test_thermo_work_and_area(built_lib, oracle, prec, shape):
+    """Square lattice with a ramped F(t) (records every 0.01 s, then held) and
+    the drive's work / area datasets, deterministic noise, against the oracle.
+    dF/dt is computed from the table slope on the device and as the
+    difference of consecutive F(t) in the oracle, so FP64 agrees to the
+    conditioning of that difference (1e-9 normwise), FP32 to 1e-4."""
+    nx, ny = shape
+    n = nx * ny
+    steps, dt, fs = 200, 0.002, 25
+    t_end = steps * dt
+    rng = np.random.default_rng(11 + n)
+    times = np.round(np.arange(0, 0.3 + 1e-9, 0.01), 10)
+    vals = np.outer(1.8 * times / 0.3, 1.0 + 0.2 * rng.random(n)).astype(complex)
+    beta0 = 0.4 * (rng.normal(size=(3, n)) + 1j * rng.normal(size=(3, n)))
+    xi = rng.normal(size=(3, steps + 1, n)) + 1j * rng.normal(size=(3, steps + 1, n))
+    n_frames = int(round(t_end / (dt * fs))) + 1
+    refs = [oracle.thermo_run(nx, ny, 1.0, 1.0, dt, 0.0, t_end, fs, n_frames, True, -0.5, 0.2, 0.0, beta0[k],
+                              F_t=(times, vals), xi=xi[k]) for k in range(3)]
+    S = refs[0]["steps"]
+    sysd = twmc.System(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=dt, frame_steps=fs, omega=-0.5, U=0.2, F=0.0,
+                       F_t=(times, vals), precision=prec, noise=twmc.NOISE_BUFFER, thermo=True)
+    tasks = sysd.make_tasks(3, t_start=0.0, t_end=t_end, ic=twmc.IC_GIVEN, init_field=beta0)
+    sysd.set_noise(xi[:, :S])
+    res = sysd.run(tasks, frames=True)
+    assert sysd.kernel_name == "ell_kernel<stencil>"
+    sysd.close()
+    check(res, refs, prec)
+    tol = 1e-9 if prec == twmc.PREC_F64 else 1e-4
+    for k, ref in enumerate(refs):
+        fw = ref["frames_written"]
+        assert np.all(res["work"][k, 0] == 0) and np.all(res["area"][k, 0] == 0)
+        for key in ("work", "area"):
+            e = rel_err(res[key][k, :fw], ref[key])
+            assert e < tol, f"traj {k} {key}: rel err {e:.3e} > {tol}"

@@ -149,3 +149,59 @@ def test_time_table_semantics(oracle):
     g = 1 + 4.0 / 3.0
     exp = np.array([[0, 1], [0, 1], [1, 1 + 0.5 * (g - 1)], [2, g], [3, g + 0.5 * (5 - g)], [4, 5], [4, 5]])
     assert np.abs(out - exp).max() < 1e-12
+
+
+def test_thermo_single_site_recursion(oracle):
+    """Work / area of a single site (no hopping, U = 0) with a ramp F(t) and
+    given noise, against the recursion written out here."""
+    dt, gamma, omega = 0.01, 1.0, -0.7
+    times = np.array([0.0, 0.3, 0.8])
+    vals = np.array([[0.0], [1.2 + 0.1j], [0.5]])
+    steps, fs = 100, 10
+    t_end = steps * dt - 1e-9
+    rng = np.random.default_rng(4)
+    xi = rng.normal(size=(steps + 2, 1)) + 1j * rng.normal(size=(steps + 2, 1))
+    b0 = np.array([0.3 - 0.2j])
+    r = oracle.thermo_run(1, 1, 0.0, gamma, dt, 0.0, t_end, fs, 11, True, omega, 0.0, 0.0, b0,
+                          F_t=(times, vals), xi=xi)
+    F = lambda t: np.interp(t, times, vals[:, 0].real) + 1j * np.interp(t, times, vals[:, 0].imag)
+    b = b0[0]
+    dt4 = np.sqrt(gamma * dt / 4)
+    t = 0.0
+    W = A = 0.0
+    work, area, frames = [0.0], [0.0], [b]
+    Fprev = F(0.0)
+    for k in range(steps):
+        Ft = F(t)
+        b = b + ((-1j * omega - gamma / 2) * b + 1j * Ft) * dt + dt4 * xi[k, 0]
+        fd = (Ft.real - Fprev.real) / dt
+        Fprev = Ft
+        W += 2 * dt * b.real * fd
+        A += dt * fd * (abs(b) ** 2 - 0.5)
+        t += dt
+        if (k + 1) % fs == 0:
+            frames.append(b)
+            work.append(W)
+            area.append(A)
+            W = A = 0.0
+    assert r["frames_written"] == 11
+    assert np.allclose(r["frames"][:, 0], frames, rtol=0, atol=1e-12)
+    assert np.allclose(r["work"][:, 0], work, rtol=0, atol=1e-12)
+    assert np.allclose(r["area"][:, 0], area, rtol=0, atol=1e-12)
+    assert abs(r["work"][1:, 0]).max() > 1e-3      # the ramp does work
+
+
+def test_thermo_without_ramp_does_no_work(oracle):
+    """A constant F(t) gives dF/dt = 0: no work, no area; the field equals the
+    base run with the same constant F."""
+    n = 16
+    rng = np.random.default_rng(5)
+    b0 = 0.3 * (rng.normal(size=n) + 1j * rng.normal(size=n))
+    xi = rng.normal(size=(60, n)) + 1j * rng.normal(size=(60, n))
+    Fc = 1.3 + 0.2j
+    times = np.array([0.0, 1.0])
+    vals = np.full((2, n), Fc)
+    r = oracle.thermo_run(4, 4, 1.0, 1.0, 0.005, 0.0, 0.25, 10, 6, True, -0.5, 0.2, 0.0, b0, F_t=(times, vals), xi=xi)
+    base = oracle.base_run(4, 4, 1.0, 1.0, 0.005, 0.0, 0.25, 10, 6, True, -0.5, 0.2, Fc, b0, xi=xi)
+    assert np.array_equal(r["frames"], base["frames"])
+    assert np.all(r["work"] == 0) and np.all(r["area"] == 0)
