@@ -663,6 +663,9 @@ int twmc_create(const twmc_system_desc* d, twmc_handle** out) {
       if (bx >= 0 && by >= 0 && square_plan(bx, by, &pv)) { h->use_fft = true; h->bx = bx; h->by = by; }
     }
     h->kname = h->use_fft ? "square_fft_kernel" : (h->lattice == TWMC_LATTICE_LIEB ? "ell_kernel<table>" : "ell_kernel<stencil>");
+    if (!h->use_fft && h->lattice == TWMC_LATTICE_SQUARE && h->prec == TWMC_PREC_F32 && h->nsites > 8192 &&
+        !h->timedep && !h->thermo)
+      h->kname = "ell_cluster_kernel";  // 2-CTA cluster per trajectory (see twmc_ell.cu use_cluster)
     rc = build_tables(h);
     *out = h;
     return rc;

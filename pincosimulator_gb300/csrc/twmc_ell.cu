@@ -103,6 +103,58 @@ bool ell_prep_t(StepArgs* a, int* grid, size_t* smem_out, std::string* err) {
   return true;
 }
 
+// 2-CTA cluster variant (square stencil, FP32, more than 8192 sites, no F(t)
+// and no work / area): launch configuration shared by both argument forms.
+constexpr int kClusterCta = 1024;
+constexpr int kClusterVariant = 7;
+
+bool use_cluster(int prec, const StepArgs& a) {
+  return prec == 0 && a.hop_kind == 1 && a.nsites > 8192 && a.nsites <= 16384 && a.ft_vals == nullptr &&
+         a.work == nullptr;
+}
+
+bool cluster_config(const void* fn, int64_t ntraj, int64_t nsites, size_t static_smem, int* grid, size_t* smem_out,
+                    std::string* err) {
+  const int64_t half = (nsites + 1) / 2, q = (half + 1) / 2;
+  const size_t smem = sizeof(float2) * 4 * size_t(q);  // two buffers of 2q slots
+  int dev = 0, sms = 0, maxsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (smem + static_smem > size_t(maxsm)) { if (err) *err = "ell cluster kernel: field does not fit"; return false; }
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) { cudaGetLastError(); if (err) *err = std::string("ell cluster smem: ") + cudaGetErrorString(e); return false; }
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(2, 1, 1);
+  cfg.blockDim = dim3(kClusterCta, 1, 1);
+  cfg.dynamicSmemBytes = smem;
+  int ncl = 0;
+  e = cudaOccupancyMaxActiveClusters(&ncl, fn, &cfg);
+  if (e != cudaSuccess || ncl <= 0) {
+    cudaGetLastError();
+    int per_sm = 0;
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kClusterCta, smem);
+    if (e != cudaSuccess || per_sm <= 0) { cudaGetLastError(); if (err) *err = "ell cluster kernel does not fit on an SM"; return false; }
+    ncl = sms * per_sm / 2;
+  }
+  *grid = 2 * int(std::min<int64_t>(ntraj, std::max(ncl, 1)));
+  *smem_out = smem;
+  return true;
+}
+
+bool cluster_launch(const StepArgs& a, cudaStream_t s, LaunchInfo* info, std::string* err) {
+  auto fn = ell_cluster_kernel<float, kClusterCta>;
+  int grid = 0;
+  size_t smem = 0;
+  if (!cluster_config(reinterpret_cast<const void*>(fn), a.ntraj, a.nsites, 0, &grid, &smem, err)) return false;
+  if (info) { info->name = "ell_cluster_kernel"; info->cta = kClusterCta; info->grid = grid; info->smem = smem; info->blocks_per_sm = 1; }
+  if (a.ntraj <= 0) return true;
+  fn<<<grid, kClusterCta, smem, s>>>(a);
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { if (err) *err = std::string("ell cluster launch: ") + cudaGetErrorString(e); return false; }
+  return true;
+}
+
 int pick_variant(int64_t n) {
   const int64_t half = (n + 1) / 2;
   int best = -1;
@@ -148,6 +200,11 @@ void ell_dev_launch(int v, const StepArgs* d, int grid, size_t smem, cudaStream_
 }  // namespace
 
 bool ell_prepare(int prec, StepArgs* a, int* variant, int* grid, size_t* smem, std::string* err) {
+  if (use_cluster(prec, *a)) {
+    *variant = kClusterVariant;
+    return cluster_config(reinterpret_cast<const void*>(ell_cluster_kernel_dev<float, kClusterCta>), a->ntraj,
+                          a->nsites, sizeof(StepArgs), grid, smem, err);
+  }
   *variant = pick_variant(a->nsites);
   if (a->hop_kind == 0)
     return prec == 0 ? ell_prep_pick<float, 0>(*variant, a, grid, smem, err)
@@ -159,7 +216,9 @@ bool ell_prepare(int prec, StepArgs* a, int* variant, int* grid, size_t* smem, s
 bool ell_launch_dev(int prec, int variant, int hop, const StepArgs* dev_args, int grid, size_t smem, cudaStream_t s,
                     std::string* err) {
   if (grid <= 0) return true;
-  if (hop == 0) {
+  if (variant == kClusterVariant) {
+    ell_cluster_kernel_dev<float, kClusterCta><<<grid, kClusterCta, smem, s>>>(dev_args);
+  } else if (hop == 0) {
     if (prec == 0) ell_dev_launch<float, 0>(variant, dev_args, grid, smem, s);
     else ell_dev_launch<double, 0>(variant, dev_args, grid, smem, s);
   } else {
@@ -172,6 +231,7 @@ bool ell_launch_dev(int prec, int variant, int hop, const StepArgs* dev_args, in
 }
 
 bool ell_launch(int prec, const StepArgs& a, cudaStream_t s, LaunchInfo* info, std::string* err) {
+  if (use_cluster(prec, a)) return cluster_launch(a, s, info, err);
   if (a.hop_kind == 0) return prec == 0 ? ell_pick<float, 0>(a, s, info, err) : ell_pick<double, 0>(a, s, info, err);
   return prec == 0 ? ell_pick<float, 1>(a, s, info, err) : ell_pick<double, 1>(a, s, info, err);
 }

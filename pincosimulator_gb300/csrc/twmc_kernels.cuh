@@ -16,6 +16,8 @@
 //   nearest-neighbour stencil -i J sum_nn beta).
 #pragma once
 
+#include <cooperative_groups.h>
+
 #include "twmc_common.cuh"
 
 namespace twmc {
@@ -499,54 +501,54 @@ __global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel
 // real-space hopping kernel (Lieb lattice, square stencil, any N)
 // Thread t of a trajectory holds VPT sites: for v < VPT/2 site t + v*TPT,
 // for v >= VPT/2 site half + t + (v - VPT/2)*TPT (half = ceil(N/2)), so the
-// two sites of one Philox call live in the same thread. Neighbour indices
-// are kept in registers as packed 16-bit pairs (N <= 16384).
-// HOP = 0: neighbour table with complex weights (h = sum_j w_j beta_j);
-// HOP = 1: square stencil h = -i J (wy (b[c+1] + b[c-1]) + wx (b[r+1] + b[r-1])).
+// two sites of one Philox call live in the same thread. Site indices are
+// recomputed from t (one multiply-add), not stored.
+// HOP = 0: neighbour table h = sum_j w_pj b[idx_pj] (Lieb couplings), the
+//          indices kept in registers as packed 16-bit pairs (N <= 16384).
+// HOP = 1: square stencil h = -i J (wy (b[c+1] + b[c-1]) + wx (b[r+1] + b[r-1])),
+//          the (row, column) of each site advanced incrementally through the
+//          thread's sites every step, so nothing per site but the field is
+//          held in registers (VPT = 16 with 1024 threads fits 64 registers).
 // ------------------------------------------------------------------------
 template <typename R, int VPT, int CTA, int HOP>
 __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_raw) {
   using T = c2_t<R>;
   constexpr int H = VPT / 2;
   T* s_b = reinterpret_cast<T*>(smem_raw);
-  const int64_t N = a.nsites;
-  const int64_t half = (N + 1) / 2;
+  const int N = int(a.nsites);
+  const int half = (N + 1) / 2;
   const int tpt = a.tpt;
   const int tpc = CTA / tpt;
   const int tid = threadIdx.x;
   const int slot = tid / tpt;
   const int t = tid % tpt;
   const bool in_slot = slot < tpc;
+  // site of slot v and whether it exists
+  auto site_of = [&](int v) -> int { return v < H ? t + v * tpt : half + t + (v - H) * tpt; };
+  auto valid_of = [&](int v) -> bool { return in_slot && (v < H ? site_of(v) < half : site_of(v) < N); };
 
-  int site[VPT];
-  bool valid[VPT];
+  uint32_t nb01[HOP == 0 ? VPT : 1], nb23[HOP == 0 ? VPT : 1];
+  // square stencil: (row, column) of the first low-half and high-half site,
+  // and the (row, column) increment of one slot (tpt sites)
+  const int nx = int(a.nx), ny = int(a.ny);
+  int rl0 = 0, cl0 = 0, rh0 = 0, ch0 = 0, dr = 0, dc = 0;
+  if constexpr (HOP == 0) {
 #pragma unroll
-  for (int v = 0; v < VPT; ++v) {
-    const int64_t s = v < H ? int64_t(t) + int64_t(v) * tpt : half + int64_t(t) + int64_t(v - H) * tpt;
-    valid[v] = in_slot && (v < H ? s < half : s < N);
-    site[v] = valid[v] ? int(s) : 0;
-  }
-  uint32_t nb01[VPT], nb23[VPT];
-#pragma unroll
-  for (int v = 0; v < VPT; ++v) {
-    const int p = site[v];
-    int n4[4];
-    if constexpr (HOP == 0) {
+    for (int v = 0; v < VPT; ++v) {
+      const int p = valid_of(v) ? site_of(v) : 0;
+      int n4[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) n4[j] = a.nbr_idx[int64_t(p) * 4 + j];
-    } else {
-      const int64_t nx = a.nx, ny = a.ny;
-      const int64_t r = p / ny, c = p % ny;
-      n4[0] = int(r * ny + (c + 1) % ny);
-      n4[1] = int(r * ny + (c + ny - 1) % ny);
-      n4[2] = int(((r + 1) % nx) * ny + c);
-      n4[3] = int(((r + nx - 1) % nx) * ny + c);
+      nb01[v] = uint32_t(n4[0]) | (uint32_t(n4[1]) << 16);
+      nb23[v] = uint32_t(n4[2]) | (uint32_t(n4[3]) << 16);
     }
-    nb01[v] = uint32_t(n4[0]) | (uint32_t(n4[1]) << 16);
-    nb23[v] = uint32_t(n4[2]) | (uint32_t(n4[3]) << 16);
+  } else {
+    rl0 = t / ny; cl0 = t % ny;
+    rh0 = (half + t) / ny; ch0 = (half + t) % ny;
+    dr = tpt / ny; dc = tpt % ny;
   }
   const T* __restrict__ g_w = reinterpret_cast<const T*>(a.nbr_w);
-  const R wy = a.ny > 1 ? R(1) : R(0), wx = a.nx > 1 ? R(1) : R(0);
+  const R wy = ny > 1 ? R(1) : R(0), wx = nx > 1 ? R(1) : R(0);
   const R J = R(a.J);
   const R dt = R(a.dt), dt4 = R(a.dt4);
   const T rsl_s = cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
@@ -567,31 +569,32 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
     const T* __restrict__ g_iF = a.iF ? reinterpret_cast<const T*>(a.iF) + tr * a.par_stride : nullptr;
     T beta[VPT];
 #pragma unroll
-    for (int v = 0; v < VPT; ++v) beta[v] = active && valid[v] ? st[site[v]] : cmake<T>(R(0), R(0));
+    for (int v = 0; v < VPT; ++v) beta[v] = active && valid_of(v) ? st[site_of(v)] : cmake<T>(R(0), R(0));
     const uint32_t seed = a.seeds[tr], id = a.ids[tr];
     const T* noise_tr = reinterpret_cast<const T*>(a.noise) + tr * a.noise_traj_stride;
     for (int64_t step = 0; step < a.nsteps; ++step) {
       const uint32_t gstep = a.step0 + uint32_t(step);
       T* sb = s_b + (a.dbuf ? buf : 0) * int64_t(tpc) * slice + int64_t(in_slot ? slot : 0) * slice;
 #pragma unroll
-      for (int v = 0; v < VPT; ++v) if (valid[v]) sb[site[v]] = beta[v];
+      for (int v = 0; v < VPT; ++v) if (valid_of(v)) sb[site_of(v)] = beta[v];
       __syncthreads();
-      // hopping term of slot v, read lazily from this step's buffer (the next
+      // hopping term of a site, read lazily from this step's buffer (the next
       // step writes the other buffer, or waits at the second barrier)
-      auto hop = [&](int v) -> T {
-        const T b0 = sb[nb01[v] & 0xFFFFu], b1 = sb[nb01[v] >> 16];
-        const T b2 = sb[nb23[v] & 0xFFFFu], b3 = sb[nb23[v] >> 16];
-        if constexpr (HOP == 0) {
-          const T* w = g_w + int64_t(site[v]) * 4;
-          T acc = cmul(__ldg(w), b0);
-          acc = cadd(acc, cmul(__ldg(w + 1), b1));
-          acc = cadd(acc, cmul(__ldg(w + 2), b2));
-          return cadd(acc, cmul(__ldg(w + 3), b3));
-        } else {
-          const T sy = cadd(b0, b1), sx = cadd(b2, b3);
-          const T s = cmake<T>(wy * sy.x + wx * sx.x, wy * sy.y + wx * sx.y);
-          return cmake<T>(J * s.y, -J * s.x);  // -i J s
-        }
+      auto hop_table = [&](int v) -> T {
+        const T b0 = sb[nb01[HOP == 0 ? v : 0] & 0xFFFFu], b1 = sb[nb01[HOP == 0 ? v : 0] >> 16];
+        const T b2 = sb[nb23[HOP == 0 ? v : 0] & 0xFFFFu], b3 = sb[nb23[HOP == 0 ? v : 0] >> 16];
+        const T* w = g_w + int64_t(site_of(v)) * 4;
+        T acc = cmul(__ldg(w), b0);
+        acc = cadd(acc, cmul(__ldg(w + 1), b1));
+        acc = cadd(acc, cmul(__ldg(w + 2), b2));
+        return cadd(acc, cmul(__ldg(w + 3), b3));
+      };
+      auto hop_stencil = [&](int p, int r, int c) -> T {
+        const int right = c + 1 < ny ? p + 1 : p + 1 - ny, left = c > 0 ? p - 1 : p - 1 + ny;
+        const int down = r + 1 < nx ? p + ny : p + ny - N, up = r > 0 ? p - ny : p - ny + N;
+        const T sy = cadd(sb[right], sb[left]), sx = cadd(sb[down], sb[up]);
+        const T s = cmake<T>(wy * sy.x + wx * sx.x, wy * sy.y + wx * sx.y);
+        return cmake<T>(J * s.y, -J * s.x);  // -i J s
       };
       int id_t = 0, id_p = 0;
       R dtt = R(0), dtp = R(0), seg_ratio = R(0);
@@ -602,22 +605,24 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
         dtp = gstep > 0 ? R(a.ft_dt[gstep - 1]) : dtt;
         if (a.work != nullptr && gstep > 0) seg_ratio = R((a.ft_dt[gstep] - a.ft_dt[gstep - 1]) / a.dt);
       }
+      int rl = rl0, cl = cl0, rh = rh0, ch = ch0;
 #pragma unroll
       for (int v = 0; v < H; ++v) {
         T xi_lo, xi_hi;
         if (a.noise_mode == 0) {
-          const u32x4 w = philox4x32_10(u32x4{uint32_t(site[v]), gstep, kStreamWiener, 0u}, seed, id);
+          const u32x4 w = philox4x32_10(u32x4{uint32_t(site_of(v)), gstep, kStreamWiener, 0u}, seed, id);
           xi_lo = normal_pair(w.x, w.y, R(0));
           xi_hi = normal_pair(w.z, w.w, R(0));
         } else {
           const T* nz = noise_tr + int64_t(gstep) * N;
-          xi_lo = nz[site[v]];
-          xi_hi = valid[v + H] ? nz[site[v + H]] : cmake<T>(R(0), R(0));
+          xi_lo = valid_of(v) ? nz[site_of(v)] : cmake<T>(R(0), R(0));
+          xi_hi = valid_of(v + H) ? nz[site_of(v + H)] : cmake<T>(R(0), R(0));
         }
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
           const int vv = q ? v + H : v;
-          const int p = site[vv];
+          const bool ok = valid_of(vv);
+          const int p = ok ? site_of(vv) : 0;
           const T r = g_rsl ? __ldg(g_rsl + p) : rsl_s;
           const T u = g_iU ? __ldg(g_iU + p) : iU_s;
           T f = g_iF ? __ldg(g_iF + p) : iF_s;
@@ -626,8 +631,11 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
             const T f1 = __ldg(reinterpret_cast<const T*>(a.ft_slopes) + int64_t(id_t) * N + p);
             f = cmake<T>(f0.x + dtt * f1.x, f0.y + dtt * f1.y);
           }
-          beta[vv] = local_update(beta[vv], hop(vv), r, u, f, dt, dt4, q ? xi_hi : xi_lo);
-          if (a.work != nullptr && valid[vv] && active) {
+          T h;
+          if constexpr (HOP == 0) h = hop_table(vv);
+          else h = ok ? (q ? hop_stencil(p, rh, ch) : hop_stencil(p, rl, cl)) : cmake<T>(R(0), R(0));
+          beta[vv] = local_update(beta[vv], h, r, u, f, dt, dt4, q ? xi_hi : xi_lo);
+          if (a.work != nullptr && ok && active) {
             R fd = R(0);
             if (timedep && gstep > 0) {  // Re F = Im(i F); the first step of a run has F(t - dt) = F(t)
               if (id_p == id_t) {
@@ -647,13 +655,17 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
             *ar += (dt * fd) * (b.x * b.x + b.y * b.y - R(0.5));
           }
         }
+        if constexpr (HOP == 1) {  // advance both sites by tpt
+          cl += dc; rl += dr; if (cl >= ny) { cl -= ny; ++rl; }
+          ch += dc; rh += dr; if (ch >= ny) { ch -= ny; ++rh; }
+        }
       }
       if (a.dbuf) buf ^= 1; else __syncthreads();
     }
     if (active) {
       bool bad = false;
 #pragma unroll
-      for (int v = 0; v < VPT; ++v) if (valid[v]) { st[site[v]] = beta[v]; bad |= !finite_c(beta[v]); }
+      for (int v = 0; v < VPT; ++v) if (valid_of(v)) { st[site_of(v)] = beta[v]; bad |= !finite_c(beta[v]); }
       set_status(a.status, traj, bad);
     }
   }
@@ -675,6 +687,139 @@ __global__ void __launch_bounds__(CTA) ell_kernel_dev(const StepArgs* __restrict
     reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(ap)[i];
   __syncthreads();
   ell_body<R, VPT, CTA, HOP>(s_a, smem_raw);
+}
+
+// ------------------------------------------------------------------------
+// Square stencil on a 2-CTA thread-block cluster per trajectory, for lattices
+// whose field does not fit one CTA's double-buffered shared memory with
+// registers to spare (N > 8192 sites, FP32). The sites are paired as in the
+// single-CTA kernel (p and p + half share a Philox call); rank 0 of the
+// cluster owns the pairs with p in [0, q), rank 1 those with p in [q, half),
+// q = ceil(half / 2), so each CTA holds two contiguous quarters of the
+// lattice. Each CTA keeps its sites in two shared-memory buffers (slots
+// [0, q) low sites, [q, 2q) their partners); a step reads the current buffer
+// -- neighbours owned by the other CTA through distributed shared memory --
+// and writes the next one, then the cluster synchronises once. The field is
+// never held in registers, so a thread loops over its pairs without
+// unrolling and 1024 threads fit 64 registers. Per-site parameters and both
+// noise modes as in the single-CTA kernel; no F(t) and no work / area.
+// ------------------------------------------------------------------------
+template <typename R, int CTA>
+__device__ __forceinline__ void ell_cluster_body(const StepArgs& a, unsigned char* smem_raw) {
+  namespace cg = cooperative_groups;
+  using T = c2_t<R>;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = int(cl.block_rank());
+  const int N = int(a.nsites), half = (N + 1) / 2, q = (half + 1) / 2;
+  const int lo0 = rank == 0 ? 0 : q;
+  const int npair = rank == 0 ? q : half - q;
+  const int nx = int(a.nx), ny = int(a.ny);
+  const R wy = ny > 1 ? R(1) : R(0), wx = nx > 1 ? R(1) : R(0);
+  const R J = R(a.J), dt = R(a.dt), dt4 = R(a.dt4);
+  const T rsl_s = cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
+  const T iU_s = cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
+  const T iF_s = cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
+  T* const own0 = reinterpret_cast<T*>(smem_raw);
+  T* const own1 = own0 + 2 * q;
+  T* const peer0 = cl.map_shared_rank(own0, rank ^ 1);
+  T* const peer1 = cl.map_shared_rank(own1, rank ^ 1);
+  const int t = threadIdx.x;
+  const int rl0 = (lo0 + t) / ny, cl0 = (lo0 + t) % ny;
+  const int rh0 = (lo0 + t + half) / ny, ch0 = (lo0 + t + half) % ny;
+  const int dr = CTA / ny, dc = CTA % ny;
+  // field value of site p in buffer b (owner and slot from the pairing)
+  auto load = [&](int b, int p) -> T {
+    const bool hi = p >= half;
+    const int lo = hi ? p - half : p;
+    const int owner = lo < q ? 0 : 1;
+    const int slot = (hi ? q : 0) + lo - (owner ? q : 0);
+    return owner == rank ? (b ? own1 : own0)[slot] : (b ? peer1 : peer0)[slot];
+  };
+  const int64_t nclusters = gridDim.x / 2;
+  for (int64_t tr = blockIdx.x / 2; tr < a.ntraj; tr += nclusters) {
+    T* st = reinterpret_cast<T*>(a.state) + tr * N;
+    const T* __restrict__ g_rsl = a.rsl ? reinterpret_cast<const T*>(a.rsl) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iU = a.iU ? reinterpret_cast<const T*>(a.iU) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iF = a.iF ? reinterpret_cast<const T*>(a.iF) + tr * a.par_stride : nullptr;
+    const uint32_t seed = a.seeds[tr], id = a.ids[tr];
+    const T* noise_tr = reinterpret_cast<const T*>(a.noise) + tr * a.noise_traj_stride;
+    for (int j = t; j < npair; j += CTA) {
+      const int pl = lo0 + j, ph = pl + half;
+      own0[j] = st[pl];
+      if (ph < N) own0[q + j] = st[ph];
+    }
+    cl.sync();
+    int b = 0;
+    bool bad = false;
+    for (int64_t step = 0; step < a.nsteps; ++step) {
+      const uint32_t gstep = a.step0 + uint32_t(step);
+      int rl = rl0, cl_ = cl0, rh = rh0, ch = ch0;  // (row, column) of this thread's pair
+#pragma unroll 1
+      for (int j = t; j < npair; j += CTA) {
+        const int pl = lo0 + j, ph = pl + half;
+        T xi_lo, xi_hi;
+        if (a.noise_mode == 0) {
+          const u32x4 w = philox4x32_10(u32x4{uint32_t(pl), gstep, kStreamWiener, 0u}, seed, id);
+          xi_lo = normal_pair(w.x, w.y, R(0));
+          xi_hi = normal_pair(w.z, w.w, R(0));
+        } else {
+          const T* nz = noise_tr + int64_t(gstep) * N;
+          xi_lo = nz[pl];
+          xi_hi = ph < N ? nz[ph] : cmake<T>(R(0), R(0));
+        }
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          const int p = k ? ph : pl;
+          if (p >= N) continue;
+          const int r = k ? rh : rl, c = k ? ch : cl_;
+          const int right = c + 1 < ny ? p + 1 : p + 1 - ny, left = c > 0 ? p - 1 : p - 1 + ny;
+          const int down = r + 1 < nx ? p + ny : p + ny - N, up = r > 0 ? p - ny : p - ny + N;
+          const T sy = cadd(load(b, right), load(b, left)), sx = cadd(load(b, down), load(b, up));
+          const T sv = cmake<T>(wy * sy.x + wx * sx.x, wy * sy.y + wx * sx.y);
+          const T h = cmake<T>(J * sv.y, -J * sv.x);  // -i J s
+          const T rr = g_rsl ? __ldg(g_rsl + p) : rsl_s;
+          const T uu = g_iU ? __ldg(g_iU + p) : iU_s;
+          const T ff = g_iF ? __ldg(g_iF + p) : iF_s;
+          const int slot = (k ? q : 0) + j;
+          (b ? own0 : own1)[slot] = local_update((b ? own1 : own0)[slot], h, rr, uu, ff, dt, dt4, k ? xi_hi : xi_lo);
+        }
+        cl_ += dc; rl += dr; if (cl_ >= ny) { cl_ -= ny; ++rl; }
+        ch += dc; rh += dr; if (ch >= ny) { ch -= ny; ++rh; }
+      }
+      b ^= 1;
+      cl.sync();
+    }
+    for (int j = t; j < npair; j += CTA) {
+      const int pl = lo0 + j, ph = pl + half;
+      const T* fin = b ? own1 : own0;
+      const T v0 = fin[j];
+      st[pl] = v0;
+      bad |= !finite_c(v0);
+      if (ph < N) {
+        const T v1 = fin[q + j];
+        st[ph] = v1;
+        bad |= !finite_c(v1);
+      }
+    }
+    set_status(a.status, tr, bad);
+    __syncthreads();  // the write-back reads buffer b before the next trajectory loads buffer 0
+  }
+}
+
+template <typename R, int CTA>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(CTA, 1) ell_cluster_kernel(const StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ell_cluster_body<R, CTA>(a, smem_raw);
+}
+
+template <typename R, int CTA>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(CTA, 1) ell_cluster_kernel_dev(const StepArgs* __restrict__ ap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) StepArgs s_a;
+  for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += CTA)
+    reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(ap)[i];
+  __syncthreads();
+  ell_cluster_body<R, CTA>(s_a, smem_raw);
 }
 
 }  // namespace twmc

@@ -21,6 +21,7 @@ POINTS = [
     dict(nx=32, ny=32, U=0.45, omega=1.5, F=0.3, n_traj=21, seed0=50, id0=1),
     dict(nx=6, ny=10, U=0.2, omega=0.0, F=1.0, n_traj=13, seed0=60, id0=1),   # no FFT plan: real space
     dict(nx=1, ny=50, U=0.2, omega=0.0, F=1.0, n_traj=11, seed0=70, id0=1),   # no FFT plan: real space
+    dict(nx=128, ny=128, U=0.2, omega=-0.5, F=1.5, n_traj=5, seed0=80, id0=1),  # 2-CTA cluster kernel
 ]
 DT, FS = 0.002, 50
 

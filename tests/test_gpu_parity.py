@@ -36,6 +36,29 @@ def test_square_stencil_parity(built_lib, oracle, shape, prec):
     check(res, refs, prec)
 
 
+@pytest.mark.parametrize("shape", [(128, 128), (96, 128), (99, 101), (1, 16384)])
+def test_cluster_stencil_parity(built_lib, oracle, shape):
+    """Lattices above 8192 sites (FP32) run on the 2-CTA cluster kernel, the
+    neighbours of the other CTA's quarters read through distributed shared
+    memory; odd N leaves the last pair without its high site."""
+    nx, ny = shape
+    res, refs = square_case(oracle, nx, ny, ntraj=3, prec=twmc.PREC_F32, hop=twmc.HOP_STENCIL, steps=60,
+                            frame_steps=20)
+    assert res["kernel"] == "ell_cluster_kernel"
+    check(res, refs, twmc.PREC_F32)
+
+
+def test_cluster_per_site_parameters(built_lib, oracle):
+    rng = np.random.default_rng(6)
+    n = 128 * 128
+    omega = -0.5 + 0.2 * rng.normal(size=n)
+    F = 1.0 + 0.3 * rng.normal(size=n) + 0.1j
+    res, refs = square_case(oracle, 128, 128, ntraj=2, prec=twmc.PREC_F32, hop=twmc.HOP_STENCIL, omega=omega, F=F,
+                            steps=40, frame_steps=20)
+    assert res["kernel"] == "ell_cluster_kernel"
+    check(res, refs, twmc.PREC_F32)
+
+
 def test_nonpow2_falls_back_to_real_space(built_lib, oracle):
     res, refs = square_case(oracle, 6, 10, ntraj=2, prec=twmc.PREC_F32, hop=twmc.HOP_FFT)
     assert res["kernel"] == "ell_kernel<stencil>"
