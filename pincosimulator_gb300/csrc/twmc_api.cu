@@ -412,6 +412,7 @@ int advance(twmc_handle* h, int64_t n, bool want_nk) {
   a.nbr_idx = h->d_nbr_idx.as<int>();
   a.nbr_w = h->d_nbr_w.p;
   a.J = h->J;
+  a.f_J = float(h->J);
   if (h->timedep) {
     a.ft_vals = h->d_ft_vals.p;
     a.ft_slopes = h->d_ft_slopes.p;

@@ -30,6 +30,41 @@ template <typename T> __device__ __forceinline__ T cmulc(T a, T b) { return cmak
 template <typename T> __device__ __forceinline__ T cmul_mi(T a) { return cmake<T>(a.y, -a.x); }
 template <typename T> __device__ __forceinline__ T cmul_pi(T a) { return cmake<T>(-a.y, a.x); }
 
+// Shared-memory access through 32-bit shared-window addresses (the
+// real-space kernels compute their neighbour indices at run time; keeping the
+// address arithmetic in 32 bits avoids 64-bit integer work per access).
+__device__ __forceinline__ uint32_t smem_addr(const void* p) {
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+__device__ __forceinline__ float2 lds_c(uint32_t a, float2) {
+  float2 v;
+  asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ double2 lds_c(uint32_t a, double2) {
+  double2 v;
+  asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(a) : "memory");
+  return v;
+}
+__device__ __forceinline__ void sts_c(uint32_t a, float2 v) {
+  asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(v.x), "f"(v.y) : "memory");
+}
+__device__ __forceinline__ void sts_c(uint32_t a, double2 v) {
+  asm volatile("st.shared.v2.f64 [%0], {%1, %2};" ::"r"(a), "d"(v.x), "d"(v.y) : "memory");
+}
+// The same address in the shared memory of cluster CTA `rank`, and a load
+// through it (distributed shared memory).
+__device__ __forceinline__ uint32_t cluster_addr(uint32_t a, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ float2 ldc_c(uint32_t a, float2) {
+  float2 v;
+  asm volatile("ld.shared::cluster.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
+  return v;
+}
+
 // Compile-time loop: f(std::integral_constant<int, I>) for I = 0..N-1.
 template <class F, int... Is>
 __device__ __forceinline__ void static_for_impl(F&& f, std::integer_sequence<int, Is...>) {

@@ -354,6 +354,7 @@ void fill_args(const twmc_hbatch* b, size_t i, StepArgs* a) {
   a->ny = d.ny;
   a->hop_kind = 1;
   a->J = d.J;
+  a->f_J = float(d.J);
 }
 
 }  // namespace

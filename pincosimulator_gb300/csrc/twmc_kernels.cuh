@@ -40,7 +40,8 @@ struct StepArgs {
   double rsl_s[2], iU_s[2], iF_s[2];
   double dt, dt4;
   float f_par[6];         // FP32 copies of rsl_s, iU_s, iF_s
-  float f_dt, f_dt4;
+  float f_dt, f_dt4;      // (FP32 kernels read these: a double-to-float conversion
+  float f_J;              //  re-done inside a loop runs on the narrow FP64 pipe)
   // noise
   int noise_mode;         // 0 Philox, 1 buffer
   const void* noise;      // [ntraj][noise_steps][N] complex (R)
@@ -549,11 +550,12 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
   }
   const T* __restrict__ g_w = reinterpret_cast<const T*>(a.nbr_w);
   const R wy = ny > 1 ? R(1) : R(0), wx = nx > 1 ? R(1) : R(0);
-  const R J = R(a.J);
-  const R dt = R(a.dt), dt4 = R(a.dt4);
-  const T rsl_s = cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
-  const T iU_s = cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
-  const T iF_s = cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
+  constexpr bool F32 = sizeof(R) == 4;
+  const R J = F32 ? R(a.f_J) : R(a.J);
+  const R dt = F32 ? R(a.f_dt) : R(a.dt), dt4 = F32 ? R(a.f_dt4) : R(a.dt4);
+  const T rsl_s = F32 ? cmake<T>(R(a.f_par[0]), R(a.f_par[1])) : cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
+  const T iU_s = F32 ? cmake<T>(R(a.f_par[2]), R(a.f_par[3])) : cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
+  const T iF_s = F32 ? cmake<T>(R(a.f_par[4]), R(a.f_par[5])) : cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
   const bool timedep = a.ft_vals != nullptr;
 
   const int64_t ngroups = (a.ntraj + tpc - 1) / tpc;
@@ -575,14 +577,16 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
     for (int64_t step = 0; step < a.nsteps; ++step) {
       const uint32_t gstep = a.step0 + uint32_t(step);
       T* sb = s_b + (a.dbuf ? buf : 0) * int64_t(tpc) * slice + int64_t(in_slot ? slot : 0) * slice;
+      const uint32_t sba = smem_addr(sb);
+      auto ld_site = [&](int q) -> T { return lds_c(sba + uint32_t(q) * uint32_t(sizeof(T)), T{}); };
 #pragma unroll
-      for (int v = 0; v < VPT; ++v) if (valid_of(v)) sb[site_of(v)] = beta[v];
+      for (int v = 0; v < VPT; ++v) if (valid_of(v)) sts_c(sba + uint32_t(site_of(v)) * uint32_t(sizeof(T)), beta[v]);
       __syncthreads();
       // hopping term of a site, read lazily from this step's buffer (the next
       // step writes the other buffer, or waits at the second barrier)
       auto hop_table = [&](int v) -> T {
-        const T b0 = sb[nb01[HOP == 0 ? v : 0] & 0xFFFFu], b1 = sb[nb01[HOP == 0 ? v : 0] >> 16];
-        const T b2 = sb[nb23[HOP == 0 ? v : 0] & 0xFFFFu], b3 = sb[nb23[HOP == 0 ? v : 0] >> 16];
+        const T b0 = ld_site(int(nb01[HOP == 0 ? v : 0] & 0xFFFFu)), b1 = ld_site(int(nb01[HOP == 0 ? v : 0] >> 16));
+        const T b2 = ld_site(int(nb23[HOP == 0 ? v : 0] & 0xFFFFu)), b3 = ld_site(int(nb23[HOP == 0 ? v : 0] >> 16));
         const T* w = g_w + int64_t(site_of(v)) * 4;
         T acc = cmul(__ldg(w), b0);
         acc = cadd(acc, cmul(__ldg(w + 1), b1));
@@ -592,7 +596,7 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
       auto hop_stencil = [&](int p, int r, int c) -> T {
         const int right = c + 1 < ny ? p + 1 : p + 1 - ny, left = c > 0 ? p - 1 : p - 1 + ny;
         const int down = r + 1 < nx ? p + ny : p + ny - N, up = r > 0 ? p - ny : p - ny + N;
-        const T sy = cadd(sb[right], sb[left]), sx = cadd(sb[down], sb[up]);
+        const T sy = cadd(ld_site(right), ld_site(left)), sx = cadd(ld_site(down), ld_site(up));
         const T s = cmake<T>(wy * sy.x + wx * sx.x, wy * sy.y + wx * sx.y);
         return cmake<T>(J * s.y, -J * s.x);  // -i J s
       };
@@ -715,14 +719,17 @@ __device__ __forceinline__ void ell_cluster_body(const StepArgs& a, unsigned cha
   const int npair = rank == 0 ? q : half - q;
   const int nx = int(a.nx), ny = int(a.ny);
   const R wy = ny > 1 ? R(1) : R(0), wx = nx > 1 ? R(1) : R(0);
-  const R J = R(a.J), dt = R(a.dt), dt4 = R(a.dt4);
-  const T rsl_s = cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
-  const T iU_s = cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
-  const T iF_s = cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
+  constexpr bool F32 = sizeof(R) == 4;
+  const R J = F32 ? R(a.f_J) : R(a.J);
+  const R dt = F32 ? R(a.f_dt) : R(a.dt), dt4 = F32 ? R(a.f_dt4) : R(a.dt4);
+  const T rsl_s = F32 ? cmake<T>(R(a.f_par[0]), R(a.f_par[1])) : cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
+  const T iU_s = F32 ? cmake<T>(R(a.f_par[2]), R(a.f_par[3])) : cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
+  const T iF_s = F32 ? cmake<T>(R(a.f_par[4]), R(a.f_par[5])) : cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
   T* const own0 = reinterpret_cast<T*>(smem_raw);
   T* const own1 = own0 + 2 * q;
-  T* const peer0 = cl.map_shared_rank(own0, rank ^ 1);
-  T* const peer1 = cl.map_shared_rank(own1, rank ^ 1);
+  constexpr uint32_t TS = uint32_t(sizeof(T));
+  const uint32_t oa0 = smem_addr(own0), oa1 = smem_addr(own1);
+  const uint32_t pa0 = cluster_addr(oa0, uint32_t(rank ^ 1)), pa1 = cluster_addr(oa1, uint32_t(rank ^ 1));
   const int t = threadIdx.x;
   const int rl0 = (lo0 + t) / ny, cl0 = (lo0 + t) % ny;
   const int rh0 = (lo0 + t + half) / ny, ch0 = (lo0 + t + half) % ny;
@@ -733,7 +740,8 @@ __device__ __forceinline__ void ell_cluster_body(const StepArgs& a, unsigned cha
     const int lo = hi ? p - half : p;
     const int owner = lo < q ? 0 : 1;
     const int slot = (hi ? q : 0) + lo - (owner ? q : 0);
-    return owner == rank ? (b ? own1 : own0)[slot] : (b ? peer1 : peer0)[slot];
+    return owner == rank ? lds_c((b ? oa1 : oa0) + uint32_t(slot) * TS, T{})
+                         : ldc_c((b ? pa1 : pa0) + uint32_t(slot) * TS, T{});
   };
   const int64_t nclusters = gridDim.x / 2;
   for (int64_t tr = blockIdx.x / 2; tr < a.ntraj; tr += nclusters) {
@@ -781,7 +789,8 @@ __device__ __forceinline__ void ell_cluster_body(const StepArgs& a, unsigned cha
           const T uu = g_iU ? __ldg(g_iU + p) : iU_s;
           const T ff = g_iF ? __ldg(g_iF + p) : iF_s;
           const int slot = (k ? q : 0) + j;
-          (b ? own0 : own1)[slot] = local_update((b ? own1 : own0)[slot], h, rr, uu, ff, dt, dt4, k ? xi_hi : xi_lo);
+          const T cur = lds_c((b ? oa1 : oa0) + uint32_t(slot) * TS, T{});
+          sts_c((b ? oa0 : oa1) + uint32_t(slot) * TS, local_update(cur, h, rr, uu, ff, dt, dt4, k ? xi_hi : xi_lo));
         }
         cl_ += dc; rl += dr; if (cl_ >= ny) { cl_ -= ny; ++rl; }
         ch += dc; rh += dr; if (ch >= ny) { ch -= ny; ++rh; }
