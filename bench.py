@@ -168,6 +168,68 @@ def make_system(twmc, hop=None, precision=None):
                        hop=twmc.HOP_FFT if hop is None else hop, n_moment_blocks=32)
 
 
+def measure_other_paths(twmc, torch):
+    """Throughput of the other configurations, one timed unit each: the
+    headline workload on the real-space stencil kernel (the same hopping
+    operator applied without the FFT), the 256-point heterogeneous batch
+    (chains of 32..1024 sites and 16..128 square lattices, 512..4096
+    trajectories per point, one frame of 250 steps in one graph launch), and
+    the 1-D Lieb lattice (256 cells, U disorder, F(t) ramp, 8192 trajectories,
+    1000 steps through twmc_run)."""
+    import numpy as np
+    out = {}
+    sysd = make_system(twmc, hop=twmc.HOP_STENCIL)
+    sysd.batch_init(sysd.make_tasks(NTRAJ, t_start=0.0, t_end=T_END, seed0=5, id0=1))
+    sysd.advance(FRAME_STEPS)
+    sysd.sync()
+    ext = torch.cuda.ExternalStream(sysd.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(2):
+        sysd.advance(FRAME_STEPS)
+    e1.record(ext)
+    sysd.sync()
+    ms = e0.elapsed_time(e1) / 2
+    out["headline_real_space"] = {"value": FRAME_STEPS * NTRAJ * NX * NY / (ms / 1e3), "unit": METRIC,
+                                  "kernel": sysd.kernel_name, "ms_per_frame": ms}
+    sysd.close()
+    rng = np.random.default_rng(3)
+    kinds = [(1, n) for n in (32, 64, 128, 256, 512, 1024)] + [(l, l) for l in (16, 32, 64, 128)]
+    pts = []
+    for _ in range(256):
+        nx, ny = kinds[rng.integers(len(kinds))]
+        pts.append(dict(nx=nx, ny=ny, U=rng.uniform(0.05, 0.5), omega=rng.uniform(-2, 2), F=rng.uniform(0, 3),
+                        dt=DT, n_traj=int(np.exp(rng.uniform(np.log(512), np.log(4096)))),
+                        seed0=int(rng.integers(1, 2 ** 31)), id0=1))
+    sites = sum(p["nx"] * p["ny"] * p["n_traj"] for p in pts)
+    hb = twmc.HBatch(pts, FRAME_STEPS, tune=True)
+    hb.run(1)
+    hb.sync()
+    hb.run(1)
+    ms = hb.sync()
+    out["heterogeneous_batch"] = {"value": FRAME_STEPS * sites / (ms / 1e3), "unit": METRIC, "points": len(pts),
+                                  "ms_per_frame": ms, "autotuned": True}
+    hb.close()
+    nc = 256
+    n = 3 * nc
+    times = np.round(np.arange(0, 40 + 1e-9, 0.01), 10)
+    vals = np.zeros((len(times), n), dtype=complex)
+    vals[:, 1::3] = (2.5 * times / 40.0)[:, None]
+    sysd = twmc.System(lattice=twmc.LATTICE_LIEB, nx=1, ny=nc, pbc=True, J_AB=1.0, J_BC=1.0, gamma=1.0,
+                       detuning=0.0, dt=DT, frame_steps=250, omega=0.0,
+                       U=twmc.Noisy(0.27, twmc.DISORDER_UNIFORM, 0.06), F=0.0, F_t=(times, vals),
+                       beta_init_sigma=0.5)
+    tasks = sysd.make_tasks(8192, t_end=2.0, store_initial=False)
+    sysd.run(tasks, frames=False, final=False)
+    t0 = time.perf_counter()
+    sysd.run(tasks, frames=False, final=False)
+    el = time.perf_counter() - t0
+    out["lieb"] = {"value": n * 8192 * 1000 / el, "unit": METRIC, "kernel": sysd.kernel_name,
+                   "timing": "host wall clock around twmc_run (initial draws and frame bookkeeping included)"}
+    sysd.close()
+    return out
+
+
 def measure_f64(twmc, torch, steps=2):
     """The same workload in the engine's FP64 mode (FP64 state, FFT and noise:
     the plain FP64 GPU split-step), device-timed like the headline."""
@@ -260,6 +322,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm-start time-to-steady-state leg")
     ap.add_argument("--no-f64", action="store_true", help="skip timing the FP64 mode")
+    ap.add_argument("--no-other", action="store_true", help="skip the other configurations")
     ap.add_argument("--ntraj", type=int, default=NTRAJ, help="profiling cases only; the bench line uses 16384")
     args = ap.parse_args()
     rank, world, local = env_rank()
@@ -366,6 +429,9 @@ def main():
     if world == 1 and args.ntraj == NTRAJ and not args.no_f64:
         f64 = measure_f64(twmc, torch)
         f64["fp32_speedup"] = value / f64["value"]
+    other = None
+    if world == 1 and args.ntraj == NTRAJ and not args.no_other:
+        other = measure_other_paths(twmc, torch)
     hbm = peaks.get("hbm_gbs")
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
@@ -381,6 +447,7 @@ def main():
         "issue": issue, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu, "clocks": clocks,
         "trajectories_per_s": value / (NX * NY * (T_END / DT)), "finite": finite,
         "kernel_ms": kernel_ms, "time_to_steady_state": warm, "fp64_mode": f64,
+        "other_paths": other,
     }
     print(json.dumps(line), flush=True)
     if dist:

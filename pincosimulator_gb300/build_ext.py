@@ -23,7 +23,7 @@ FLAGS = ["-O3", "-lineinfo", "-std=c++17", "--expt-relaxed-constexpr", "-Xcompil
          "-Xcompiler", "-fvisibility=hidden", "-DNDEBUG", "-I", os.path.join(HERE, "..", "include")]
 SOURCES = ["twmc_api.cu", "twmc_square_f32.cu", "twmc_square_f64.cu", "twmc_ell.cu", "twmc_misc.cu",
            "twmc_noalloc.cu", "twmc_hbatch.cu",
-           "twmc_mlp.cu"]
+           "twmc_mlp.cu", "twmc_ell_fast.cu"]
 
 
 def _write_plans() -> None:

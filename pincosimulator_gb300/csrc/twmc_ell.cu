@@ -1,112 +1,25 @@
-// twmc_ell.cu -- launcher of the real-space (neighbour list / stencil) step kernel.
+// twmc_ell.cu -- launcher of the real-space (neighbour list / stencil) step kernel:
+// general path (F(t), work / area, noise buffer; FP32 and FP64), the 2-CTA
+// cluster kernel, and the dispatch to the FP32 fast path (twmc_ell_fast.cu).
 #include <algorithm>
 #include <string>
 
-#include "twmc_kernels.cuh"
-#include "twmc_launch.h"
+#include "twmc_ell_impl.cuh"
 
 namespace twmc {
 
 namespace {
-template <typename R, int VPT, int CTA, int HOP>
-bool ell_launch_t(const StepArgs& a0, cudaStream_t s, LaunchInfo* info, std::string* err) {
-  StepArgs a = a0;
-  const int64_t half = (a.nsites + 1) / 2;
-  const int tpt = int((half + VPT / 2 - 1) / (VPT / 2));
-  if (tpt > CTA) { if (err) *err = "ell kernel: lattice too large for this variant"; return false; }
-  a.tpt = tpt;
-  const int tpc = CTA / tpt;
-  using T = c2_t<R>;
-  auto fn = ell_kernel<R, VPT, CTA, HOP>;
-  int dev = 0, sms = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  int maxsm = 0;
-  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  size_t smem = sizeof(T) * size_t(2) * tpc * size_t(a.nsites);
-  a.dbuf = 1;
-  if (smem > size_t(maxsm)) { smem /= 2; a.dbuf = 0; }
-  if (smem > size_t(maxsm)) { if (err) *err = "ell kernel: trajectory does not fit in shared memory"; return false; }
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e != cudaSuccess) { cudaGetLastError(); if (err) *err = std::string("ell smem: ") + cudaGetErrorString(e); return false; }
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, CTA, smem);
-  if (e != cudaSuccess || per_sm <= 0) { cudaGetLastError(); if (err) *err = "ell kernel does not fit on an SM"; return false; }
-  const int64_t groups = (a.ntraj + tpc - 1) / tpc;
-  const int grid = int(std::min<int64_t>(groups, int64_t(sms) * per_sm));
-  if (info) { info->name = "ell_kernel"; info->cta = CTA; info->grid = grid; info->smem = smem; info->blocks_per_sm = per_sm; }
-  if (grid <= 0) return true;
-  fn<<<grid, CTA, smem, s>>>(a);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) { if (err) *err = std::string("ell launch: ") + cudaGetErrorString(e); return false; }
-  return true;
-}
-
-// Variants (sites per thread, threads per CTA); the launcher picks the one
-// with the fewest idle site slots (ties: fewer sites per thread).
-constexpr int kVariants[][2] = {{2, 256}, {4, 256}, {6, 256}, {8, 256}, {8, 512}, {8, 1024}, {16, 1024}};
-
-template <typename R, int HOP>
-bool ell_pick(const StepArgs& a, cudaStream_t s, LaunchInfo* info, std::string* err) {
-  const int64_t n = a.nsites, half = (n + 1) / 2;
-  int best = -1;
-  double best_u = -1.0;
-  for (int i = 0; i < int(sizeof(kVariants) / sizeof(kVariants[0])); ++i) {
-    const int vpt = kVariants[i][0], cta = kVariants[i][1];
-    const int64_t tpt = (half + vpt / 2 - 1) / (vpt / 2);
-    if (tpt > cta) continue;
-    const int64_t tpc = cta / tpt;
-    const double u = double(n * tpc) / double(int64_t(cta) * vpt);
-    if (u > best_u + 1e-9) { best_u = u; best = i; }
-  }
-  switch (best) {
-    case 0: return ell_launch_t<R, 2, 256, HOP>(a, s, info, err);
-    case 1: return ell_launch_t<R, 4, 256, HOP>(a, s, info, err);
-    case 2: return ell_launch_t<R, 6, 256, HOP>(a, s, info, err);
-    case 3: return ell_launch_t<R, 8, 256, HOP>(a, s, info, err);
-    case 4: return ell_launch_t<R, 8, 512, HOP>(a, s, info, err);
-    case 5: return ell_launch_t<R, 8, 1024, HOP>(a, s, info, err);
-    case 6: return ell_launch_t<R, 16, 1024, HOP>(a, s, info, err);
-    default: break;
-  }
-  if (err) *err = "ell kernel: more than 16384 sites per trajectory";
-  return false;
-}
-// Configuration of the device-argument variant (ell_kernel_dev): sets a->tpt
-// and a->dbuf, returns grid and shared-memory size.
-template <typename R, int VPT, int CTA, int HOP>
-bool ell_prep_t(StepArgs* a, int* grid, size_t* smem_out, std::string* err) {
-  const int64_t half = (a->nsites + 1) / 2;
-  const int tpt = int((half + VPT / 2 - 1) / (VPT / 2));
-  if (tpt > CTA) { if (err) *err = "ell kernel: lattice too large for this variant"; return false; }
-  a->tpt = tpt;
-  const int tpc = CTA / tpt;
-  using T = c2_t<R>;
-  auto fn = ell_kernel_dev<R, VPT, CTA, HOP>;
-  int dev = 0, sms = 0, maxsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const int avail = maxsm - int(sizeof(StepArgs)) - 64;
-  size_t smem = sizeof(T) * size_t(2) * tpc * size_t(a->nsites);
-  a->dbuf = 1;
-  if (smem > size_t(avail)) { smem /= 2; a->dbuf = 0; }
-  if (smem > size_t(avail)) { if (err) *err = "ell kernel: trajectory does not fit in shared memory"; return false; }
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e != cudaSuccess) { cudaGetLastError(); if (err) *err = std::string("ell smem: ") + cudaGetErrorString(e); return false; }
-  int per_sm = 0;
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, CTA, smem);
-  if (e != cudaSuccess || per_sm <= 0) { cudaGetLastError(); if (err) *err = "ell kernel does not fit on an SM"; return false; }
-  const int64_t groups = (a->ntraj + tpc - 1) / tpc;
-  *grid = int(std::min<int64_t>(groups, int64_t(sms) * per_sm));
-  *smem_out = smem;
-  return true;
-}
-
+using namespace ell_impl;
 // 2-CTA cluster variant (square stencil, FP32, more than 8192 sites, no F(t)
 // and no work / area): launch configuration shared by both argument forms.
 constexpr int kClusterCta = 1024;
 constexpr int kClusterVariant = 7;
+constexpr int kFastOffset = 16;  // variant ids of the FP32 fast path (twmc_ell_fast.cu)
+
+// Runs without F(t), work / area or a noise buffer take the fast path (FP32).
+bool use_fast(int prec, const StepArgs& a) {
+  return prec == 0 && a.ft_vals == nullptr && a.work == nullptr && a.noise_mode == 0;
+}
 
 bool use_cluster(int prec, const StepArgs& a) {
   return prec == 0 && a.hop_kind == 1 && a.nsites > 8192 && a.nsites <= 16384 && a.ft_vals == nullptr &&
@@ -155,48 +68,6 @@ bool cluster_launch(const StepArgs& a, cudaStream_t s, LaunchInfo* info, std::st
   return true;
 }
 
-int pick_variant(int64_t n) {
-  const int64_t half = (n + 1) / 2;
-  int best = -1;
-  double best_u = -1.0;
-  for (int i = 0; i < int(sizeof(kVariants) / sizeof(kVariants[0])); ++i) {
-    const int vpt = kVariants[i][0], cta = kVariants[i][1];
-    const int64_t tpt = (half + vpt / 2 - 1) / (vpt / 2);
-    if (tpt > cta) continue;
-    const int64_t tpc = cta / tpt;
-    const double u = double(n * tpc) / double(int64_t(cta) * vpt);
-    if (u > best_u + 1e-9) { best_u = u; best = i; }
-  }
-  return best;
-}
-
-template <typename R, int HOP>
-bool ell_prep_pick(int v, StepArgs* a, int* grid, size_t* smem, std::string* err) {
-  switch (v) {
-    case 0: return ell_prep_t<R, 2, 256, HOP>(a, grid, smem, err);
-    case 1: return ell_prep_t<R, 4, 256, HOP>(a, grid, smem, err);
-    case 2: return ell_prep_t<R, 6, 256, HOP>(a, grid, smem, err);
-    case 3: return ell_prep_t<R, 8, 256, HOP>(a, grid, smem, err);
-    case 4: return ell_prep_t<R, 8, 512, HOP>(a, grid, smem, err);
-    case 5: return ell_prep_t<R, 8, 1024, HOP>(a, grid, smem, err);
-    case 6: return ell_prep_t<R, 16, 1024, HOP>(a, grid, smem, err);
-    default: if (err) *err = "ell kernel: more than 16384 sites per trajectory"; return false;
-  }
-}
-
-template <typename R, int HOP>
-void ell_dev_launch(int v, const StepArgs* d, int grid, size_t smem, cudaStream_t s) {
-  switch (v) {
-    case 0: ell_kernel_dev<R, 2, 256, HOP><<<grid, 256, smem, s>>>(d); break;
-    case 1: ell_kernel_dev<R, 4, 256, HOP><<<grid, 256, smem, s>>>(d); break;
-    case 2: ell_kernel_dev<R, 6, 256, HOP><<<grid, 256, smem, s>>>(d); break;
-    case 3: ell_kernel_dev<R, 8, 256, HOP><<<grid, 256, smem, s>>>(d); break;
-    case 4: ell_kernel_dev<R, 8, 512, HOP><<<grid, 512, smem, s>>>(d); break;
-    case 5: ell_kernel_dev<R, 8, 1024, HOP><<<grid, 1024, smem, s>>>(d); break;
-    case 6: ell_kernel_dev<R, 16, 1024, HOP><<<grid, 1024, smem, s>>>(d); break;
-    default: break;
-  }
-}
 }  // namespace
 
 bool ell_prepare(int prec, StepArgs* a, int* variant, int* grid, size_t* smem, std::string* err) {
@@ -206,11 +77,16 @@ bool ell_prepare(int prec, StepArgs* a, int* variant, int* grid, size_t* smem, s
                           a->nsites, sizeof(StepArgs), grid, smem, err);
   }
   *variant = pick_variant(a->nsites);
+  if (use_fast(prec, *a)) {
+    const int v = *variant;
+    *variant = v + kFastOffset;
+    return ell_prepare_fast_f32(v, a, grid, smem, err);
+  }
   if (a->hop_kind == 0)
-    return prec == 0 ? ell_prep_pick<float, 0>(*variant, a, grid, smem, err)
-                     : ell_prep_pick<double, 0>(*variant, a, grid, smem, err);
-  return prec == 0 ? ell_prep_pick<float, 1>(*variant, a, grid, smem, err)
-                   : ell_prep_pick<double, 1>(*variant, a, grid, smem, err);
+    return prec == 0 ? ell_prep_pick<float, 0, false>(*variant, a, grid, smem, err)
+                     : ell_prep_pick<double, 0, false>(*variant, a, grid, smem, err);
+  return prec == 0 ? ell_prep_pick<float, 1, false>(*variant, a, grid, smem, err)
+                   : ell_prep_pick<double, 1, false>(*variant, a, grid, smem, err);
 }
 
 bool ell_launch_dev(int prec, int variant, int hop, const StepArgs* dev_args, int grid, size_t smem, cudaStream_t s,
@@ -218,12 +94,14 @@ bool ell_launch_dev(int prec, int variant, int hop, const StepArgs* dev_args, in
   if (grid <= 0) return true;
   if (variant == kClusterVariant) {
     ell_cluster_kernel_dev<float, kClusterCta><<<grid, kClusterCta, smem, s>>>(dev_args);
+  } else if (variant >= kFastOffset) {
+    ell_launch_dev_fast_f32(variant - kFastOffset, hop, dev_args, grid, smem, s);
   } else if (hop == 0) {
-    if (prec == 0) ell_dev_launch<float, 0>(variant, dev_args, grid, smem, s);
-    else ell_dev_launch<double, 0>(variant, dev_args, grid, smem, s);
+    if (prec == 0) ell_dev_launch<float, 0, false>(variant, dev_args, grid, smem, s);
+    else ell_dev_launch<double, 0, false>(variant, dev_args, grid, smem, s);
   } else {
-    if (prec == 0) ell_dev_launch<float, 1>(variant, dev_args, grid, smem, s);
-    else ell_dev_launch<double, 1>(variant, dev_args, grid, smem, s);
+    if (prec == 0) ell_dev_launch<float, 1, false>(variant, dev_args, grid, smem, s);
+    else ell_dev_launch<double, 1, false>(variant, dev_args, grid, smem, s);
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) { if (err) *err = std::string("ell launch: ") + cudaGetErrorString(e); return false; }
@@ -232,8 +110,10 @@ bool ell_launch_dev(int prec, int variant, int hop, const StepArgs* dev_args, in
 
 bool ell_launch(int prec, const StepArgs& a, cudaStream_t s, LaunchInfo* info, std::string* err) {
   if (use_cluster(prec, a)) return cluster_launch(a, s, info, err);
-  if (a.hop_kind == 0) return prec == 0 ? ell_pick<float, 0>(a, s, info, err) : ell_pick<double, 0>(a, s, info, err);
-  return prec == 0 ? ell_pick<float, 1>(a, s, info, err) : ell_pick<double, 1>(a, s, info, err);
+  if (use_fast(prec, a)) return ell_launch_fast_f32(a, s, info, err);
+  if (a.hop_kind == 0)
+    return prec == 0 ? ell_pick<float, 0, false>(a, s, info, err) : ell_pick<double, 0, false>(a, s, info, err);
+  return prec == 0 ? ell_pick<float, 1, false>(a, s, info, err) : ell_pick<double, 1, false>(a, s, info, err);
 }
 
 }  // namespace twmc

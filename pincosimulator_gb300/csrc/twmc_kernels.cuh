@@ -510,8 +510,10 @@ __global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel
 //          the (row, column) of each site advanced incrementally through the
 //          thread's sites every step, so nothing per site but the field is
 //          held in registers (VPT = 16 with 1024 threads fits 64 registers).
+// FAST: the common run (Philox noise, no F(t), no work / area) with those
+//       features compiled out instead of tested per site.
 // ------------------------------------------------------------------------
-template <typename R, int VPT, int CTA, int HOP>
+template <typename R, int VPT, int CTA, int HOP, bool FAST = false>
 __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_raw) {
   using T = c2_t<R>;
   constexpr int H = VPT / 2;
@@ -556,7 +558,7 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
   const T rsl_s = F32 ? cmake<T>(R(a.f_par[0]), R(a.f_par[1])) : cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
   const T iU_s = F32 ? cmake<T>(R(a.f_par[2]), R(a.f_par[3])) : cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
   const T iF_s = F32 ? cmake<T>(R(a.f_par[4]), R(a.f_par[5])) : cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
-  const bool timedep = a.ft_vals != nullptr;
+  const bool timedep = !FAST && a.ft_vals != nullptr;
 
   const int64_t ngroups = (a.ntraj + tpc - 1) / tpc;
   const int64_t slice = N;
@@ -607,13 +609,13 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
         dtt = R(a.ft_dt[gstep]);
         id_p = gstep > 0 ? a.ft_id[gstep - 1] : id_t;
         dtp = gstep > 0 ? R(a.ft_dt[gstep - 1]) : dtt;
-        if (a.work != nullptr && gstep > 0) seg_ratio = R((a.ft_dt[gstep] - a.ft_dt[gstep - 1]) / a.dt);
+        if (!FAST && a.work != nullptr && gstep > 0) seg_ratio = R((a.ft_dt[gstep] - a.ft_dt[gstep - 1]) / a.dt);
       }
       int rl = rl0, cl = cl0, rh = rh0, ch = ch0;
 #pragma unroll
       for (int v = 0; v < H; ++v) {
         T xi_lo, xi_hi;
-        if (a.noise_mode == 0) {
+        if (FAST || a.noise_mode == 0) {
           const u32x4 w = philox4x32_10(u32x4{uint32_t(site_of(v)), gstep, kStreamWiener, 0u}, seed, id);
           xi_lo = normal_pair(w.x, w.y, R(0));
           xi_hi = normal_pair(w.z, w.w, R(0));
@@ -639,7 +641,7 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
           if constexpr (HOP == 0) h = hop_table(vv);
           else h = ok ? (q ? hop_stencil(p, rh, ch) : hop_stencil(p, rl, cl)) : cmake<T>(R(0), R(0));
           beta[vv] = local_update(beta[vv], h, r, u, f, dt, dt4, q ? xi_hi : xi_lo);
-          if (a.work != nullptr && ok && active) {
+          if (!FAST && a.work != nullptr && ok && active) {
             R fd = R(0);
             if (timedep && gstep > 0) {  // Re F = Im(i F); the first step of a run has F(t - dt) = F(t)
               if (id_p == id_t) {
@@ -675,22 +677,22 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
   }
 }
 
-template <typename R, int VPT, int CTA, int HOP>
+template <typename R, int VPT, int CTA, int HOP, bool FAST>
 __global__ void __launch_bounds__(CTA) ell_kernel(const StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ell_body<R, VPT, CTA, HOP>(a, smem_raw);
+  ell_body<R, VPT, CTA, HOP, FAST>(a, smem_raw);
 }
 
 // Same, with the arguments in device memory (kept there across the frames of a
 // captured graph); they are copied to shared memory first.
-template <typename R, int VPT, int CTA, int HOP>
+template <typename R, int VPT, int CTA, int HOP, bool FAST>
 __global__ void __launch_bounds__(CTA) ell_kernel_dev(const StepArgs* __restrict__ ap) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(16) StepArgs s_a;
   for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += CTA)
     reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(ap)[i];
   __syncthreads();
-  ell_body<R, VPT, CTA, HOP>(s_a, smem_raw);
+  ell_body<R, VPT, CTA, HOP, FAST>(s_a, smem_raw);
 }
 
 // ------------------------------------------------------------------------

@@ -40,6 +40,11 @@ bool square_launch_f64(int bx, int by, const StepArgs& a, int nparams, cudaStrea
 
 // Real-space (neighbour list / stencil) step kernel, any N.
 bool ell_launch(int prec, const StepArgs& a, cudaStream_t s, LaunchInfo* info, std::string* err);
+// FP32 fast path of the real-space kernel (twmc_ell_fast.cu): variant = index
+// of the (sites per thread, threads per CTA) table.
+bool ell_launch_fast_f32(const StepArgs& a, cudaStream_t s, LaunchInfo* info, std::string* err);
+bool ell_prepare_fast_f32(int variant, StepArgs* a, int* grid, size_t* smem, std::string* err);
+void ell_launch_dev_fast_f32(int variant, int hop, const StepArgs* dev_args, int grid, size_t smem, cudaStream_t s);
 
 // One-off kernels (twmc_misc.cu).
 struct InitArgs {
