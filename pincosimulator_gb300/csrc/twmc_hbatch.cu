@@ -88,7 +88,7 @@ int hb_tpc(int shape) {
 
 template <class P>
 __device__ __forceinline__ void hb_run(unsigned char* smem, const StepArgs& a, bool reload, int64_t group, int& buf) {
-  SquareGroup<float, P, HB_CTA> g(smem);
+  SquareGroup<float, P, HB_CTA, true> g(smem);  // batch points: Philox noise, scalar U, F
   if (reload) {
     g.load_tables(a);
     __syncthreads();

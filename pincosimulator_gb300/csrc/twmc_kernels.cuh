@@ -294,8 +294,9 @@ struct SquareCfg {
 // One square-lattice trajectory group (TPC trajectories) for a.nsteps steps:
 // the body of square_fft_kernel, shared with the heterogeneous-batch kernel.
 // Shared memory: twiddles | 2 padded exchange buffers | state slices (FP32) |
-// separable k-space table.
-template <typename R, class P, int CTA>
+// separable k-space table. FAST: Philox noise and scalar U, F (per-site
+// omega allowed) compiled in instead of tested per site.
+template <typename R, class P, int CTA, bool FAST = false>
 struct SquareGroup {
   using T = c2_t<R>;
   using I = PlanInfo<P>;
@@ -348,7 +349,7 @@ struct SquareGroup {
   __device__ __forceinline__ void run(const StepArgs& a, int64_t g, int& buf) {
     const T* tw0 = s_tw;
     const T* tw1 = s_tw + I::TW0;
-    const bool has_rsl = a.rsl != nullptr, has_iU = a.iU != nullptr, has_iF = a.iF != nullptr;
+    const bool has_rsl = a.rsl != nullptr, has_iU = !FAST && a.iU != nullptr, has_iF = !FAST && a.iF != nullptr;
     // thread parts of the k-space indices in the last pass's layout
     const int ky_t = I::bitrev(pos_thr[LAST] & ((1 << P::by) - 1), P::by);
     const int kx_t = P::bx ? I::bitrev(pos_thr[LAST] >> P::by, P::bx) : 0;
@@ -418,7 +419,7 @@ struct SquareGroup {
         constexpr int s_lo = decltype(Q)::value;          // top slot bit clear
         constexpr int s_hi = s_lo | (E / 2);
         T xi_lo, xi_hi;
-        if (a.noise_mode == 0) {
+        if (FAST || a.noise_mode == 0) {
           const int p = pos_thr[0] | I::pos_reg(0, s_lo);  // p < N/2
           const u32x4 w = philox4x32_10(u32x4{uint32_t(p), gstep, kStreamWiener, 0u}, seed, id);
           xi_lo = normal_pair(w.x, w.y, R(0));
@@ -486,10 +487,10 @@ struct SquareGroup {
   }
 };
 
-template <typename R, class P, int CTA>
+template <typename R, class P, int CTA, bool FAST = false>
 __global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel(const StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  using G = SquareGroup<R, P, CTA>;
+  using G = SquareGroup<R, P, CTA, FAST>;
   G grp(smem_raw);
   grp.load_tables(a);
   __syncthreads();

@@ -23,7 +23,7 @@ constexpr int cta_for() {
   return tpc * tpt;
 }
 
-template <typename R, class P>
+template <typename R, class P, bool FAST>
 bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo* info, std::string* err) {
   constexpr int CTA = cta_for<R, P>();
   using Cfg = SquareCfg<P, CTA, R>;
@@ -38,7 +38,7 @@ bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo*
                     std::to_string(maxsm) + ")";
     return false;
   }
-  auto fn = square_fft_kernel<R, P, CTA>;
+  auto fn = square_fft_kernel<R, P, CTA, FAST>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -76,8 +76,12 @@ bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo*
 template <typename R>
 bool square_dispatch(int bx, int by, const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo* info,
                      std::string* err) {
-#define TWMC_SHAPE(BX, BY) \
-  if (bx == BX && by == BY) return square_launch_t<R, Plan_##BX##_##BY>(a, nparams, s, info, err);
+  // FP32 runs with Philox noise and scalar U, F take the fast instantiation
+  const bool fast = sizeof(R) == 4 && a.noise_mode == 0 && a.iU == nullptr && a.iF == nullptr;
+#define TWMC_SHAPE(BX, BY)                                                                          \
+  if (bx == BX && by == BY)                                                                         \
+    return fast ? square_launch_t<R, Plan_##BX##_##BY, sizeof(R) == 4>(a, nparams, s, info, err)   \
+                : square_launch_t<R, Plan_##BX##_##BY, false>(a, nparams, s, info, err);
   TWMC_SHAPE(0, 5) TWMC_SHAPE(0, 6) TWMC_SHAPE(0, 7) TWMC_SHAPE(0, 8) TWMC_SHAPE(0, 9) TWMC_SHAPE(0, 10)
   TWMC_SHAPE(0, 11) TWMC_SHAPE(0, 12) TWMC_SHAPE(4, 4) TWMC_SHAPE(5, 5) TWMC_SHAPE(6, 6)
 #undef TWMC_SHAPE
