@@ -94,6 +94,7 @@ struct twmc_handle {
   bool timedep = false;
   bool thermo = false;     // work / area accumulators (TWMCThermoSolver)
   DevBuf d_work, d_area;
+  DevBuf d_wide;           // FP32 -> FP64 download staging (bounded chunk)
   std::vector<double> ft_times;   // with sentinel
   std::vector<cd> ft_vals, ft_slopes;
   // kernel selection
@@ -569,17 +570,29 @@ int download_real(twmc_handle* h, const DevBuf& b, double* out, size_t n) {
   return TWMC_OK;
 }
 
+// The batch's field as complex128 into host memory. FP32 state is widened on
+// the GPU in chunks of at most kWideChunk doubles (a bounded per-handle
+// buffer), each chunk copied straight to its place in `out`.
+constexpr size_t kWideChunk = size_t(1) << 25;  // 256 MB of doubles
+
 int download_field(twmc_handle* h, double* out) {
   const size_t n = size_t(h->ntraj * h->nsites);
   if (h->prec) {
     TWMC_CUDA(h, cudaMemcpyAsync(out, h->d_state.p, n * 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     TWMC_CUDA(h, cudaStreamSynchronize(h->stream));
-  } else {
-    std::vector<float> tmp(2 * n);
-    TWMC_CUDA(h, cudaMemcpyAsync(tmp.data(), h->d_state.p, n * 2 * sizeof(float), cudaMemcpyDeviceToHost, h->stream));
-    TWMC_CUDA(h, cudaStreamSynchronize(h->stream));
-    for (size_t i = 0; i < 2 * n; ++i) out[i] = double(tmp[i]);
+    return TWMC_OK;
   }
+  const size_t total = 2 * n;
+  const size_t chunk = std::min(total, kWideChunk);
+  if (!h->d_wide.ensure(chunk * sizeof(double))) return fail(h, TWMC_ERR_NOMEM, "download buffer allocation");
+  const float* src = static_cast<const float*>(h->d_state.p);
+  for (size_t off = 0; off < total; off += chunk) {
+    const size_t m = std::min(chunk, total - off);
+    std::string err;
+    if (!widen_launch(src + off, h->d_wide.as<double>(), int64_t(m), h->stream, &err)) return fail(h, TWMC_ERR_CUDA, err);
+    TWMC_CUDA(h, cudaMemcpyAsync(out + off, h->d_wide.p, m * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+  }
+  TWMC_CUDA(h, cudaStreamSynchronize(h->stream));
   return TWMC_OK;
 }
 
@@ -900,11 +913,18 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
       }
       TWMC_CUDA(h, cudaStreamSynchronize(h->stream));
       if (out && out->final_field) {
-        fbuf.resize(size_t(bn * N * 2));
-        rc = download_field(h, fbuf.data());
-        if (rc) return rc;
-        for (size_t i = 0; i < bn; ++i)
-          std::memcpy(out->final_field + idx[i] * N * 2, &fbuf[i * N * 2], sizeof(double) * size_t(N * 2));
+        bool contiguous = true;  // tasks of this group in consecutive output rows: download in place
+        for (size_t i = 1; i < bn && contiguous; ++i) contiguous = idx[i] == idx[0] + i;
+        if (contiguous) {
+          rc = download_field(h, out->final_field + idx[0] * N * 2);
+          if (rc) return rc;
+        } else {
+          fbuf.resize(size_t(bn * N * 2));
+          rc = download_field(h, fbuf.data());
+          if (rc) return rc;
+          for (size_t i = 0; i < bn; ++i)
+            std::memcpy(out->final_field + idx[i] * N * 2, &fbuf[i * N * 2], sizeof(double) * size_t(N * 2));
+        }
       }
       std::vector<int> st(bn);
       TWMC_CUDA(h, cudaMemcpy(st.data(), h->d_status.p, bn * sizeof(int), cudaMemcpyDeviceToHost));

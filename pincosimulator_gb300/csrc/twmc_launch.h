@@ -74,6 +74,8 @@ struct InitArgs {
   double gamma, detuning;
 };
 bool init_launch(const InitArgs& a, cudaStream_t s, std::string* err);
+// out[k] = double(in[k]) for k < n (in: FP32 device array).
+bool widen_launch(const void* in, double* out, int64_t n, cudaStream_t s, std::string* err);
 
 struct MomentArgs {
   int64_t ntraj, nsites;

@@ -109,6 +109,13 @@ bool check(cudaError_t e, std::string* err, const char* what) {
   return false;
 }
 
+// FP32 -> FP64 widening of a field (complex64 -> complex128 as 2n reals),
+// so that downloads copy the caller's type directly.
+__global__ void widen_kernel(const float* __restrict__ in, double* __restrict__ out, int64_t n) {
+  for (int64_t k = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; k < n; k += int64_t(gridDim.x) * blockDim.x)
+    out[k] = double(in[k]);
+}
+
 }  // namespace
 
 bool init_launch(const InitArgs& a, cudaStream_t s, std::string* err) {
@@ -159,6 +166,15 @@ bool philox_launch(const uint32_t* d_ctr, size_t n, uint32_t k0, uint32_t k1, ui
   if (n == 0) return true;
   philox_kernel<<<unsigned((n + 255) / 256), 256, 0, s>>>(d_ctr, n, k0, k1, d_out);
   return check(cudaGetLastError(), err, "philox_kernel");
+}
+
+bool widen_launch(const void* in, double* out, int64_t n, cudaStream_t s, std::string* err) {
+  if (n <= 0) return true;
+  const int grid = int(std::min<int64_t>((n + 255) / 256, 152 * 16));
+  widen_kernel<<<grid, 256, 0, s>>>(static_cast<const float*>(in), out, n);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) { if (err) *err = std::string("widen: ") + cudaGetErrorString(e); return false; }
+  return true;
 }
 
 }  // namespace twmc

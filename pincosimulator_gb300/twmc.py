@@ -293,23 +293,37 @@ class System:
         self._noise = xi
         self._check(self.lib.twmc_set_noise_buffer(self.h, xi.ctypes.data, xi.size))
 
-    def run(self, tasks, *, frames=True, final=True, moments=False, realizations=False, n_frames=None):
-        """twmc_run: returns a dict of numpy arrays."""
+    def run(self, tasks, *, frames=True, final=True, moments=False, realizations=False, n_frames=None,
+            buffers: Optional[dict] = None):
+        """twmc_run: returns a dict of numpy arrays. `buffers` may supply
+        preallocated C-contiguous arrays for "frames", "final" and "moments"
+        (e.g. views of pinned host memory reused across calls); the others are
+        allocated here."""
         n = len(tasks)
         N = self.n_sites
         if n_frames is None:
             dt_obs = self.desc.dt * self.desc.frame_steps
             n_frames = max(int(round((t.t_end - t.t_start) / dt_obs)) + int(t.store_initial) for t in tasks)
+        buffers = buffers or {}
+
+        def buf(key, shape, dtype):
+            b = buffers.get(key)
+            if b is None:
+                return np.zeros(shape, dtype=dtype)
+            if b.shape != shape or b.dtype != dtype or not b.flags["C_CONTIGUOUS"]:
+                raise ValueError(f"buffer {key}: need C-contiguous {dtype} of shape {shape}")
+            return b
+
         out = Outputs()
         res = {}
         if frames:
-            res["frames"] = np.zeros((n, n_frames, N), dtype=np.complex128)
+            res["frames"] = buf("frames", (n, n_frames, N), np.complex128)
             out.frames = res["frames"].ctypes.data
         if final:
-            res["final"] = np.zeros((n, N), dtype=np.complex128)
+            res["final"] = buf("final", (n, N), np.complex128)
             out.final_field = res["final"].ctypes.data
         if moments:
-            res["moments"] = np.zeros((n_frames, self.n_blocks, N, 3), dtype=np.float64)
+            res["moments"] = buf("moments", (n_frames, self.n_blocks, N, 3), np.float64)
             out.moments = res["moments"].ctypes.data
         if realizations:
             for key in ("U_realization", "omega_realization", "F_realization"):
