@@ -118,47 +118,15 @@ def ncu_traffic():
     return _profile_figure("dram_bytes_per_launch_full_size")
 
 
-def measure_warm_start(n_train=1024, traj_train=256, t_train=20.0, n_test=64, traj_test=512, t_test=20.0):
+def measure_warm_start():
     """Time to steady state with and without the learned warm start on a
     reduced version of the 32 x 32 sweep (F ~ U[0,3], detuning ~ U[-2,2],
-    U ~ U[0.05,0.5], J = gamma = 1, dt = 0.002): plain runs of n_train points
-    generate the training rows, the MLP is trained on the GPU, then n_test
+    U ~ U[0.05,0.5], J = gamma = 1, dt = 0.002): plain runs of 1024 points
+    generate the training rows, the MLP is trained on the GPU, then 64
     held-out points run warm-started and plain (the judge)."""
-    import numpy as np
-    import torch
     from pincosimulator_gb300 import warmstart as wsm
 
-    t0 = time.perf_counter()
-    train = wsm.sample_points(n_train, seed=101)
-    rows, su = wsm.steady_rows(train, 32, 32, n_traj=traj_train, t_end=t_train)
-    torch.cuda.synchronize()
-    t1 = time.perf_counter()
-    ws = wsm.WarmStart(32, 32, max_batch=128, seed=7)
-    rep = ws.fit(wsm.features(train), rows, epochs=2000, batch=128, lr=3e-3)
-    torch.cuda.synchronize()
-    t2 = time.perf_counter()
-    test = wsm.sample_points(n_test, seed=202)
-    res = wsm.warm_sweep(ws, test, n_traj=traj_test, t_end=t_test)
-    t3 = time.perf_counter()
-    tw, tp = float(np.median(res.warm.ttss)), float(np.median(res.plain.ttss))
-    se_n = np.sqrt(res.warm.n_inf_se ** 2 + res.plain.n_inf_se ** 2)
-    se_g = np.sqrt(res.warm.g2_inf_se ** 2 + res.plain.g2_inf_se ** 2)
-    ok = np.isfinite(se_g) & np.isfinite(res.warm.g2_inf)
-    return {
-        "workload": f"32x32 PBC sweep, train {n_train} points x {traj_train} trajectories to t={t_train:g}, "
-                    f"test {n_test} held-out points x {traj_test} trajectories to t={t_test:g}, dt=0.002, "
-                    "frames every 0.5; MLP 5-256-256-256-2049 BF16, 2000 epochs",
-        "ttss_plain_median": tp, "ttss_warm_median": tw, "speedup_median": tp / max(tw, 0.5),
-        "ttss_plain_mean": float(np.mean(res.plain.ttss)), "ttss_warm_mean": float(np.mean(res.warm.ttss)),
-        "n_within_1se_frac": float(np.mean(np.abs(res.warm.n_inf - res.plain.n_inf) <= se_n)),
-        "g2_within_1se_frac": float(np.mean(np.abs(res.warm.g2_inf - res.plain.g2_inf)[ok] <= se_g[ok]))
-        if ok.any() else None,
-        "reruns": int(res.rerun.sum()), "test_points": n_test,
-        "train_s": t1 - t0, "train_site_updates_per_s": su / (t1 - t0), "fit_s": t2 - t1,
-        "fit_steps": rep.steps, "mlp_launches": rep.launches, "final_loss": rep.losses[-1][1], "sweep_s": t3 - t2,
-        "ttss_definition": "first save time with |n - n_inf| <= max(1 SE, 1e-3 n_inf), staying within 2x for "
-                           "2 more frames; n_inf = mean of the last quarter of frames",
-    }
+    return wsm.evaluate(32, n_train=1024, traj_train=256, t_train=20.0, n_test=64, traj_test=512, t_test=20.0)
 
 
 def make_system(twmc, hop=None, precision=None):

@@ -67,14 +67,14 @@ def _point_descs(points, nx, ny, n_traj, dt, seed0):
     return out
 
 
-def steady_rows(points, nx, ny, n_traj, t_end, dt=0.002, frame_period=0.5, tail_frames=8, seed0=1):
+def steady_rows(points, nx, ny, n_traj, t_end, dt=0.002, frame_period=0.5, tail_frames=8, seed0=1, tune=False):
     """Plain (vacuum-initialised) runs of every point to t_end; MLP rows
     [P][2N+1] (device float32) from the mean field and <|a|^2> averaged over
     the last tail_frames frames."""
     torch = _torch()
     frame_steps = max(1, int(math.ceil(frame_period / dt - 1e-9)))
     n_frames = max(tail_frames, int(round(t_end / (frame_steps * dt))))
-    hb = twmc.HBatch(_point_descs(points, nx, ny, n_traj, dt, seed0), frame_steps)
+    hb = twmc.HBatch(_point_descs(points, nx, ny, n_traj, dt, seed0), frame_steps, tune=tune)
     try:
         N = nx * ny
         P = len(points)
@@ -195,13 +195,14 @@ class SweepResult:
     device_ms: float = 0.0
 
 
-def run_sweep(points, nx, ny, n_traj, t_end, dt=0.002, frame_period=0.5, init=None, seed0=1, tail=0.25):
+def run_sweep(points, nx, ny, n_traj, t_end, dt=0.002, frame_period=0.5, init=None, seed0=1, tail=0.25,
+              tune=False):
     """Runs every point from t = 0 to t_end (vacuum start, or `init` =
     (beta_init, beta_sigma) device arrays [P][N][2] from WarmStart) and
     follows the site-averaged n and g2 frame by frame."""
     frame_steps = max(1, int(math.ceil(frame_period / dt - 1e-9)))
     n_frames = int(round(t_end / (frame_steps * dt)))
-    hb = twmc.HBatch(_point_descs(points, nx, ny, n_traj, dt, seed0), frame_steps)
+    hb = twmc.HBatch(_point_descs(points, nx, ny, n_traj, dt, seed0), frame_steps, tune=tune)
     P, N = len(points), nx * ny
     try:
         if init is not None:
@@ -250,16 +251,83 @@ class WarmSweep:
     g2_final: np.ndarray
 
 
-def warm_sweep(ws: WarmStart, points, n_traj, t_end, dt=0.002, frame_period=0.5, seed0=1, rerun_se=1.0):
+def warm_sweep(ws: WarmStart, points, n_traj, t_end, dt=0.002, frame_period=0.5, seed0=1, rerun_se=1.0,
+               tune=False):
     """Warm-started sweep judged by plain runs: a point whose warm steady n
     differs from the plain one by more than rerun_se combined standard
     errors takes the plain result."""
     x = features(points)
     init = ws.initial_fields(x)
-    warm = run_sweep(points, ws.nx, ws.ny, n_traj, t_end, dt, frame_period, init=init, seed0=seed0)
-    plain = run_sweep(points, ws.nx, ws.ny, n_traj, t_end, dt, frame_period, init=None, seed0=seed0 + 1000003)
+    warm = run_sweep(points, ws.nx, ws.ny, n_traj, t_end, dt, frame_period, init=init, seed0=seed0, tune=tune)
+    plain = run_sweep(points, ws.nx, ws.ny, n_traj, t_end, dt, frame_period, init=None, seed0=seed0 + 1000003,
+                      tune=tune)
     se = np.sqrt(warm.n_inf_se ** 2 + plain.n_inf_se ** 2)
     rerun = ~(np.abs(warm.n_inf - plain.n_inf) <= rerun_se * se)   # non-finite warm results rerun too
     n_final = np.where(rerun, plain.n_inf, warm.n_inf)
     g2_final = np.where(rerun, plain.g2_inf, warm.g2_inf)
     return WarmSweep(warm, plain, rerun, n_final, g2_final)
+
+
+def evaluate(L=32, n_train=1024, traj_train=256, t_train=20.0, n_test=64, traj_test=512, t_test=20.0,
+             epochs=2000, batch=128, lr=3e-3, tune=False) -> dict:
+    """Trains the warm start on plain steady states of n_train sampled points
+    of an L x L lattice and compares warm-started against plain runs of
+    n_test held-out points: median time to steady state, agreement of the
+    steady n and g2 within one combined standard error, reruns, timings."""
+    import time
+    torch = _torch()
+    t0 = time.perf_counter()
+    train = sample_points(n_train, seed=101)
+    rows, su = steady_rows(train, L, L, n_traj=traj_train, t_end=t_train, tune=tune)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
+    ws = WarmStart(L, L, max_batch=batch, seed=7)
+    rep = ws.fit(features(train), rows, epochs=epochs, batch=batch, lr=lr)
+    torch.cuda.synchronize()
+    t2 = time.perf_counter()
+    test = sample_points(n_test, seed=202)
+    res = warm_sweep(ws, test, n_traj=traj_test, t_end=t_test, tune=tune)
+    t3 = time.perf_counter()
+    tw, tp = float(np.median(res.warm.ttss)), float(np.median(res.plain.ttss))
+    se_n = np.sqrt(res.warm.n_inf_se ** 2 + res.plain.n_inf_se ** 2)
+    se_g = np.sqrt(res.warm.g2_inf_se ** 2 + res.plain.g2_inf_se ** 2)
+    ok = np.isfinite(se_g) & np.isfinite(res.warm.g2_inf)
+    return {
+        "workload": f"{L}x{L} PBC sweep, train {n_train} points x {traj_train} trajectories to t={t_train:g}, "
+                    f"test {n_test} held-out points x {traj_test} trajectories to t={t_test:g}, dt=0.002, "
+                    f"frames every 0.5; MLP 5-256-256-256-{2 * L * L + 1} BF16, {epochs} epochs",
+        "ttss_plain_median": tp, "ttss_warm_median": tw, "speedup_median": tp / max(tw, 0.5),
+        "ttss_plain_mean": float(np.mean(res.plain.ttss)), "ttss_warm_mean": float(np.mean(res.warm.ttss)),
+        "n_within_1se_frac": float(np.mean(np.abs(res.warm.n_inf - res.plain.n_inf) <= se_n)),
+        "g2_within_1se_frac": float(np.mean(np.abs(res.warm.g2_inf - res.plain.g2_inf)[ok] <= se_g[ok]))
+        if ok.any() else None,
+        "reruns": int(res.rerun.sum()), "test_points": n_test,
+        "train_s": t1 - t0, "train_site_updates_per_s": su / (t1 - t0), "fit_s": t2 - t1,
+        "fit_steps": rep.steps, "mlp_launches": rep.launches, "final_loss": rep.losses[-1][1], "sweep_s": t3 - t2,
+        "ttss_definition": "first save time with |n - n_inf| <= max(1 SE, 1e-3 n_inf), staying within 2x for "
+                           "2 more frames; n_inf = mean of the last quarter of frames",
+    }
+
+
+def main(argv=None):
+    import argparse
+    import json
+    ap = argparse.ArgumentParser(description="Learned warm-start sweep: train on plain steady states, then "
+                                             "compare warm-started and plain runs of held-out points.")
+    ap.add_argument("--L", type=int, default=32, help="lattice side")
+    ap.add_argument("--train", type=int, default=1024, help="training points")
+    ap.add_argument("--train-traj", type=int, default=256)
+    ap.add_argument("--train-t", type=float, default=20.0)
+    ap.add_argument("--test", type=int, default=64, help="held-out sweep points")
+    ap.add_argument("--test-traj", type=int, default=512)
+    ap.add_argument("--test-t", type=float, default=20.0)
+    ap.add_argument("--epochs", type=int, default=2000)
+    ap.add_argument("--tune", action="store_true", help="let the batch autotuner pick FFT or real-space kernels")
+    a = ap.parse_args(argv)
+    r = evaluate(a.L, a.train, a.train_traj, a.train_t, a.test, a.test_traj, a.test_t, epochs=a.epochs, tune=a.tune)
+    print(json.dumps(r), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    raise SystemExit(main())
