@@ -162,3 +162,23 @@ def test_full_size_fft_equals_stencil(built_lib):
     assert np.isfinite(fa).all()
     assert rel_err(fa, fb) < 1e-4
     assert np.allclose(ma[:, :, 0].sum(0), (np.abs(fa) ** 2).sum(0), rtol=1e-9)
+
+
+def test_run_into_caller_buffers(built_lib):
+    """run() writes into caller-provided result arrays (reused across calls,
+    e.g. pinned memory) exactly what it returns in arrays of its own; the
+    FP32 field arrives widened to complex128 (chunked on the GPU)."""
+    s = twmc.System(nx=32, ny=32, J=1.0, gamma=1.0, dt=0.002, frame_steps=25,
+                    omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=0.2, F=1.5, beta_init_sigma=0.5)
+    tasks = s.make_tasks(300, t_end=0.1, seed0=9, store_initial=False)
+    ref = s.run(tasks, frames=True, final=True, moments=True)
+    bufs = {"final": np.full((300, 1024), np.nan + 0j), "moments": np.full(ref["moments"].shape, np.nan),
+            "frames": np.full(ref["frames"].shape, np.nan + 0j)}
+    for _ in range(2):
+        got = s.run(tasks, frames=True, final=True, moments=True, buffers=bufs)
+        for k in ("final", "moments", "frames"):
+            assert got[k] is bufs[k] and np.array_equal(got[k], ref[k]), k
+    assert np.array_equal(ref["final"], ref["frames"][:, -1])
+    with pytest.raises(ValueError):
+        s.run(tasks, final=True, frames=False, buffers={"final": np.zeros((300, 1024), np.complex64)})
+    s.close()
