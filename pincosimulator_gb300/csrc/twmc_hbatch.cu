@@ -247,10 +247,16 @@ std::mutex g_tune_mu;
 using namespace twmc;
 using cd = std::complex<double>;
 
+constexpr int kEllStreams = 8;
+
 struct twmc_hbatch {
   int device = 0;
   cudaStream_t s0 = nullptr, s1 = nullptr;
   cudaEvent_t fork = nullptr, join = nullptr, e0 = nullptr, e1 = nullptr;
+  // real-space points run on kEllStreams captured streams (parallel graph
+  // branches), so that small points do not serialise behind each other
+  std::vector<cudaStream_t> ell_streams;
+  std::vector<cudaEvent_t> ell_joins;
   std::string err;
   int64_t frame_steps = 1;
   size_t npts = 0;
@@ -383,6 +389,14 @@ int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_st
   cudaStreamCreateWithFlags(&b->s1, cudaStreamNonBlocking);
   cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
   cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
+  b->ell_streams.assign(kEllStreams, nullptr);
+  b->ell_joins.assign(kEllStreams, nullptr);
+  b->ell_streams[0] = b->s1;
+  b->ell_joins[0] = b->join;
+  for (int k = 1; k < kEllStreams; ++k) {
+    cudaStreamCreateWithFlags(&b->ell_streams[k], cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&b->ell_joins[k], cudaEventDisableTiming);
+  }
   cudaEventCreate(&b->e0);
   cudaEventCreate(&b->e1);
   cudaDeviceProp prop;
@@ -586,23 +600,37 @@ int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_st
   }
 
   // capture one frame
-  cudaStream_t s0 = b->s0, s1 = b->s1;
+  cudaStream_t s0 = b->s0;
   cudaStreamSynchronize(s0);
   if (cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     return hfail(b, TWMC_ERR_CUDA, "stream capture failed to start");
   cudaEventRecord(b->fork, s0);
-  cudaStreamWaitEvent(s1, b->fork, 0);
+  for (cudaStream_t es : b->ell_streams) cudaStreamWaitEvent(es, b->fork, 0);
   std::string cerr;
   bool ok = true;
-  for (size_t i = 0; i < n && ok; ++i)
-    if (b->shape[i] < 0)
-      ok = ell_launch_dev(0, b->ell_variant[i], 1, b->args.p + i, b->ell_grid[i], b->ell_smem[i], s1, &cerr);
-  cudaEventRecord(b->join, s1);
+  {
+    // longest-processing-time-first assignment of the real-space points to
+    // the least loaded stream (load = trajectories x sites)
+    std::vector<size_t> order;
+    for (size_t i = 0; i < n; ++i) if (b->shape[i] < 0) order.push_back(i);
+    std::sort(order.begin(), order.end(), [&](size_t x, size_t y) {
+      return b->ntraj[x] * b->nsites[x] > b->ntraj[y] * b->nsites[y];
+    });
+    std::vector<double> load(b->ell_streams.size(), 0.0);
+    for (size_t i : order) {
+      if (!ok) break;
+      const size_t k = size_t(std::min_element(load.begin(), load.end()) - load.begin());
+      load[k] += double(b->ntraj[i]) * double(b->nsites[i]);
+      ok = ell_launch_dev(0, b->ell_variant[i], 1, b->args.p + i, b->ell_grid[i], b->ell_smem[i],
+                          b->ell_streams[k], &cerr);
+    }
+  }
+  for (size_t k = 0; k < b->ell_streams.size(); ++k) cudaEventRecord(b->ell_joins[k], b->ell_streams[k]);
   if (b->nitems > 0) {
     cudaMemsetAsync(b->counter.p, 0, sizeof(int), s0);
     hbatch_kernel<<<b->grid, HB_CTA, kHbSmem, s0>>>(b->args.p, b->pshape.p, b->items.p, b->nitems, b->counter.p);
   }
-  cudaStreamWaitEvent(s0, b->join, 0);
+  for (cudaEvent_t ej : b->ell_joins) cudaStreamWaitEvent(s0, ej, 0);
   dim3 mg(unsigned((b->max_sites + 127) / 128), unsigned(b->max_blocks), unsigned(n));
   hbatch_moments_kernel<<<mg, 128, 0, s0>>>(b->margs.p);
   hbatch_bump_kernel<<<unsigned((n + 127) / 128), 128, 0, s0>>>(b->args.p, int(n), uint32_t(frame_steps));
@@ -714,6 +742,10 @@ void twmc_hbatch_destroy(twmc_hbatch* b) {
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
   for (cudaEvent_t e : {b->fork, b->join, b->e0, b->e1}) if (e) cudaEventDestroy(e);
+  for (size_t k = 1; k < b->ell_streams.size(); ++k) {
+    if (b->ell_joins[k]) cudaEventDestroy(b->ell_joins[k]);
+    if (b->ell_streams[k]) cudaStreamDestroy(b->ell_streams[k]);
+  }
   if (b->s0) cudaStreamDestroy(b->s0);
   if (b->s1) cudaStreamDestroy(b->s1);
   delete b;
