@@ -61,7 +61,9 @@ enum twmc_lattice {
 enum twmc_precision { TWMC_PREC_F32 = 0, TWMC_PREC_F64 = 1 };
 
 enum twmc_noise_mode {
-  TWMC_NOISE_PHILOX = 0, /* in-kernel Philox4x32-10 keyed by (seed, id), counter (site, step, stream) */
+  TWMC_NOISE_PHILOX = 0, /* in-kernel Philox4x32-10: Wiener increments with a fixed key and counter
+                            (site pair, step, id, seed); initial fields and disorder keyed by (seed, id),
+                            counter (site pair, 0, stream, 0) */
   TWMC_NOISE_BUFFER = 1  /* caller-supplied Wiener increments (deterministic-noise mode) */
 };
 
@@ -121,8 +123,8 @@ typedef struct twmc_system_desc {
 } twmc_system_desc;
 
 typedef struct twmc_task_desc {
-  uint64_t id;            /* TWMCTaskData::id (also the second Philox key word, low 32 bits) */
-  uint32_t seed;          /* TWMCTaskData::rngSeed (first Philox key word) */
+  uint64_t id;            /* TWMCTaskData::id (low 32 bits enter the Philox key / counter) */
+  uint32_t seed;          /* TWMCTaskData::rngSeed (Philox key / counter word) */
   int32_t ic_kind;        /* twmc_ic_kind */
   double t_start, t_end;  /* TWMCTaskData::t_start / t_end */
   int32_t store_initial;  /* TWMCTaskData::storeInitialState */

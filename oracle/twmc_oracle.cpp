@@ -77,6 +77,10 @@ void philox4x32_10(const uint32_t ctr_in[4], const uint32_t key_in[2], uint32_t 
 
 // Noise streams (counter word 2). Shared convention with the GPU solver.
 enum Stream : uint32_t { kStreamWiener = 0, kStreamInit = 1, kStreamU = 2, kStreamOmega = 3, kStreamF = 4 };
+// The Wiener stream has a fixed key (hex digits of pi) and the trajectory in
+// the counter: ctr = (site pair, step, tid, seed). The other streams use
+// key = (seed, tid), ctr = (site pair, step, stream, 0).
+constexpr uint32_t kWienerKey0 = 0x243F6A88u, kWienerKey1 = 0x85A308D3u;
 
 // Box-Muller from two 32-bit words, FP64 flavour: u = (a + 1/2) 2^-32.
 void normal_pair_f64(uint32_t a, uint32_t b, double* z0, double* z1) {
@@ -112,8 +116,9 @@ cd site_normal(uint32_t seed, uint32_t tid, uint32_t step, uint32_t stream, int6
                int f32_flavour) {
   uint32_t c0; int lane;
   site_counter(p, n, &c0, &lane);
-  const uint32_t ctr[4] = {c0, step, stream, 0u};
-  const uint32_t key[2] = {seed, tid};
+  const bool wiener = stream == kStreamWiener;
+  const uint32_t ctr[4] = {c0, step, wiener ? tid : stream, wiener ? seed : 0u};
+  const uint32_t key[2] = {wiener ? kWienerKey0 : seed, wiener ? kWienerKey1 : tid};
   uint32_t w[4];
   philox4x32_10(ctr, key, w);
   double z0, z1;

@@ -21,6 +21,8 @@ M1 = np.uint64(0xCD9E8D57)
 W0 = np.uint64(0x9E3779B9)
 W1 = np.uint64(0xBB67AE85)
 MASK = np.uint64(0xFFFFFFFF)
+# fixed key of the Wiener stream (stream 0): hex digits of pi
+WIENER_KEY = (0x243F6A88, 0x85A308D3)
 
 
 def philox4x32_10(ctr, key):
@@ -46,8 +48,12 @@ def site_normals(seed: int, tid: int, step: int, stream: int, n: int, f32_flavou
     p = np.arange(n)
     c0 = np.where(p < half, p, p - half).astype(np.uint32)
     lane = np.where(p < half, 0, 2)
-    ctr = np.stack([c0, np.full(n, step, np.uint32), np.full(n, stream, np.uint32), np.zeros(n, np.uint32)], -1)
-    key = np.broadcast_to(np.array([seed, tid], dtype=np.uint32), (n, 2))
+    if stream == 0:   # Wiener: fixed key, ctr = (site pair, step, tid, seed)
+        ctr = np.stack([c0, np.full(n, step, np.uint32), np.full(n, tid, np.uint32), np.full(n, seed, np.uint32)], -1)
+        key = np.broadcast_to(np.array(WIENER_KEY, dtype=np.uint32), (n, 2))
+    else:             # ctr = (site pair, step, stream, 0), key = (seed, tid)
+        ctr = np.stack([c0, np.full(n, step, np.uint32), np.full(n, stream, np.uint32), np.zeros(n, np.uint32)], -1)
+        key = np.broadcast_to(np.array([seed, tid], dtype=np.uint32), (n, 2))
     w = philox4x32_10(ctr, key)
     a = w[p, lane].astype(np.float64)
     b = w[p, lane + 1].astype(np.float64)

@@ -102,6 +102,18 @@ __host__ __device__ __forceinline__ u32x4 philox4x32_10(u32x4 c, uint32_t k0, ui
 // Noise streams (counter word 2).
 enum : uint32_t { kStreamWiener = 0, kStreamInit = 1, kStreamU = 2, kStreamOmega = 3, kStreamF = 4 };
 
+// Wiener increments use a fixed key, kWienerKey0/1 (hex digits of pi), and
+// carry the trajectory in the counter: (site pair, step, id, seed). The key
+// schedule is then a compile-time constant that folds into the round's
+// XORs instead of two adds per round on per-thread keys. The other streams
+// keep the key (seed, id) and the counter (site pair, 0, stream, 0); with
+// these constants the two families cannot share an input block.
+constexpr uint32_t kWienerKey0 = 0x243F6A88u, kWienerKey1 = 0x85A308D3u;
+
+__host__ __device__ __forceinline__ u32x4 wiener_words(uint32_t pair, uint32_t step, uint32_t seed, uint32_t id) {
+  return philox4x32_10(u32x4{pair, step, id, seed}, kWienerKey0, kWienerKey1);
+}
+
 // Box-Muller, FP32: u = fma(float(w), 2^-32, 2^-33) in (0, 1]; angle in [-pi, pi).
 __device__ __forceinline__ float2 normal_pair(uint32_t a, uint32_t b, float) {
   const float u1 = __fmaf_rn(__uint2float_rn(a), 0x1p-32f, 0x1p-33f);

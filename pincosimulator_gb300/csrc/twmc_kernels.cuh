@@ -421,7 +421,7 @@ struct SquareGroup {
         T xi_lo, xi_hi;
         if (FAST || a.noise_mode == 0) {
           const int p = pos_thr[0] | I::pos_reg(0, s_lo);  // p < N/2
-          const u32x4 w = philox4x32_10(u32x4{uint32_t(p), gstep, kStreamWiener, 0u}, seed, id);
+          const u32x4 w = wiener_words(uint32_t(p), gstep, seed, id);
           xi_lo = normal_pair(w.x, w.y, R(0));
           xi_hi = normal_pair(w.z, w.w, R(0));
         } else {
@@ -617,7 +617,7 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
       for (int v = 0; v < H; ++v) {
         T xi_lo, xi_hi;
         if (FAST || a.noise_mode == 0) {
-          const u32x4 w = philox4x32_10(u32x4{uint32_t(site_of(v)), gstep, kStreamWiener, 0u}, seed, id);
+          const u32x4 w = wiener_words(uint32_t(site_of(v)), gstep, seed, id);
           xi_lo = normal_pair(w.x, w.y, R(0));
           xi_hi = normal_pair(w.z, w.w, R(0));
         } else {
@@ -770,7 +770,7 @@ __device__ __forceinline__ void ell_cluster_body(const StepArgs& a, unsigned cha
         const int pl = lo0 + j, ph = pl + half;
         T xi_lo, xi_hi;
         if (a.noise_mode == 0) {
-          const u32x4 w = philox4x32_10(u32x4{uint32_t(pl), gstep, kStreamWiener, 0u}, seed, id);
+          const u32x4 w = wiener_words(uint32_t(pl), gstep, seed, id);
           xi_lo = normal_pair(w.x, w.y, R(0));
           xi_hi = normal_pair(w.z, w.w, R(0));
         } else {
