@@ -437,6 +437,7 @@ int advance(twmc_handle* h, int64_t n, bool want_nk) {
                       : square_launch_f64(h->bx, h->by, a, nparams, h->stream, &h->last_info, &err);
   } else {
     ok = ell_launch(h->prec, a, h->stream, &h->last_info, &err);
+    if (ok && std::strncmp(h->last_info.name, "ell_cluster", 11) == 0) h->kname = h->last_info.name;
   }
   cudaEventRecord(ev.second, h->stream);
   h->ev_pending.push_back(ev);

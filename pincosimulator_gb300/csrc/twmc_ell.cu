@@ -1,6 +1,6 @@
 // twmc_ell.cu -- launcher of the real-space (neighbour list / stencil) step kernel:
 // general path (F(t), work / area, noise buffer; FP32 and FP64), the 2-CTA
-// cluster kernel, and the dispatch to the FP32 fast path (twmc_ell_fast.cu).
+// cluster kernels (general and power-of-two geometry), and the dispatch to the FP32 fast path (twmc_ell_fast.cu).
 #include <algorithm>
 #include <string>
 
@@ -14,6 +14,8 @@ using namespace ell_impl;
 // and no work / area): launch configuration shared by both argument forms.
 constexpr int kClusterCta = 1024;
 constexpr int kClusterVariant = 7;
+constexpr int kClusterPow2Variant = 8;      // power-of-two geometry (general features)
+constexpr int kClusterPow2FastVariant = 9;  // power-of-two geometry, Philox noise, scalar U and F
 constexpr int kFastOffset = 16;  // variant ids of the FP32 fast path (twmc_ell_fast.cu)
 
 // Runs without F(t), work / area or a noise buffer take the fast path (FP32).
@@ -24,6 +26,20 @@ bool use_fast(int prec, const StepArgs& a) {
 bool use_cluster(int prec, const StepArgs& a) {
   return prec == 0 && a.hop_kind == 1 && a.nsites > 8192 && a.nsites <= 16384 && a.ft_vals == nullptr &&
          a.work == nullptr;
+}
+
+// Power-of-two geometry for the cluster kernel: N = 2^k, ny a power of two,
+// 2 <= ny <= N / 4 (every row inside one quarter of the lattice).
+bool cluster_pow2(const StepArgs& a) {
+  const int64_t n = a.nsites, ny = a.ny;
+  return (n & (n - 1)) == 0 && a.nx * ny == n && ny >= 2 && (ny & (ny - 1)) == 0 && ny <= n / 4;
+}
+
+bool cluster_fast(const StepArgs& a) { return a.noise_mode == 0 && a.iU == nullptr && a.iF == nullptr; }
+
+int cluster_variant(const StepArgs& a) {
+  if (!cluster_pow2(a)) return kClusterVariant;
+  return cluster_fast(a) ? kClusterPow2FastVariant : kClusterPow2Variant;
 }
 
 bool cluster_config(const void* fn, int64_t ntraj, int64_t nsites, size_t static_smem, int* grid, size_t* smem_out,
@@ -56,11 +72,17 @@ bool cluster_config(const void* fn, int64_t ntraj, int64_t nsites, size_t static
 }
 
 bool cluster_launch(const StepArgs& a, cudaStream_t s, LaunchInfo* info, std::string* err) {
-  auto fn = ell_cluster_kernel<float, kClusterCta>;
+  const int v = cluster_variant(a);
+  void (*fn)(const StepArgs) = v == kClusterPow2FastVariant ? ell_cluster_pow2_kernel<kClusterCta, true>
+                               : v == kClusterPow2Variant   ? ell_cluster_pow2_kernel<kClusterCta, false>
+                                                            : ell_cluster_kernel<float, kClusterCta>;
   int grid = 0;
   size_t smem = 0;
   if (!cluster_config(reinterpret_cast<const void*>(fn), a.ntraj, a.nsites, 0, &grid, &smem, err)) return false;
-  if (info) { info->name = "ell_cluster_kernel"; info->cta = kClusterCta; info->grid = grid; info->smem = smem; info->blocks_per_sm = 1; }
+  if (info) {
+    info->name = v == kClusterVariant ? "ell_cluster_kernel" : "ell_cluster_pow2_kernel";
+    info->cta = kClusterCta; info->grid = grid; info->smem = smem; info->blocks_per_sm = 1;
+  }
   if (a.ntraj <= 0) return true;
   fn<<<grid, kClusterCta, smem, s>>>(a);
   cudaError_t e = cudaGetLastError();
@@ -72,9 +94,11 @@ bool cluster_launch(const StepArgs& a, cudaStream_t s, LaunchInfo* info, std::st
 
 bool ell_prepare(int prec, StepArgs* a, int* variant, int* grid, size_t* smem, std::string* err) {
   if (use_cluster(prec, *a)) {
-    *variant = kClusterVariant;
-    return cluster_config(reinterpret_cast<const void*>(ell_cluster_kernel_dev<float, kClusterCta>), a->ntraj,
-                          a->nsites, sizeof(StepArgs), grid, smem, err);
+    *variant = cluster_variant(*a);
+    void (*fn)(const StepArgs*) = *variant == kClusterPow2FastVariant ? ell_cluster_pow2_kernel_dev<kClusterCta, true>
+                                  : *variant == kClusterPow2Variant   ? ell_cluster_pow2_kernel_dev<kClusterCta, false>
+                                                                      : ell_cluster_kernel_dev<float, kClusterCta>;
+    return cluster_config(reinterpret_cast<const void*>(fn), a->ntraj, a->nsites, sizeof(StepArgs), grid, smem, err);
   }
   *variant = pick_variant(a->nsites);
   if (use_fast(prec, *a)) {
@@ -94,6 +118,10 @@ bool ell_launch_dev(int prec, int variant, int hop, const StepArgs* dev_args, in
   if (grid <= 0) return true;
   if (variant == kClusterVariant) {
     ell_cluster_kernel_dev<float, kClusterCta><<<grid, kClusterCta, smem, s>>>(dev_args);
+  } else if (variant == kClusterPow2Variant) {
+    ell_cluster_pow2_kernel_dev<kClusterCta, false><<<grid, kClusterCta, smem, s>>>(dev_args);
+  } else if (variant == kClusterPow2FastVariant) {
+    ell_cluster_pow2_kernel_dev<kClusterCta, true><<<grid, kClusterCta, smem, s>>>(dev_args);
   } else if (variant >= kFastOffset) {
     ell_launch_dev_fast_f32(variant - kFastOffset, hop, dev_args, grid, smem, s);
   } else if (hop == 0) {

@@ -834,4 +834,127 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(CTA, 1) ell_cluster_
   ell_cluster_body<R, CTA>(s_a, smem_raw);
 }
 
+// ------------------------------------------------------------------------
+// Power-of-two form of the cluster stencil: N = nx * ny = 2^k sites, ny a
+// power of two with 2 <= ny <= N / 4, FP32. Same pairing, ownership and
+// shared-memory slots
+// as ell_cluster_body -- rank 0 holds the quarters ("bands") [0, q) and
+// [N/2, N/2 + q), rank 1 the other two, q = N / 4 -- but the owner / slot
+// arithmetic reduces to bits: a row lies inside one band and the bands
+// alternate between the ranks (0, 1, 0, 1, wrapping), so left / right
+// neighbours are always in the thread's own CTA, and up / down neighbours
+// are in the other CTA exactly on a band's first / last row. Sums are formed
+// in the same order as ell_cluster_body. FAST: Philox noise and scalar U, F
+// compiled in (omega per site allowed); otherwise both noise modes and
+// per-site U, F as in ell_cluster_body.
+// ------------------------------------------------------------------------
+template <int CTA, bool FAST>
+__device__ __forceinline__ void ell_cluster_pow2_body(const StepArgs& a, unsigned char* smem_raw) {
+  namespace cg = cooperative_groups;
+  using T = float2;
+  cg::cluster_group cl = cg::this_cluster();
+  const int rank = int(cl.block_rank());
+  const int N = int(a.nsites), half = N >> 1, q = N >> 2;
+  const int ny = int(a.ny), m = ny - 1;
+  const int lny = __ffs(ny) - 1;
+  const int rb_last = (q >> lny) - 1;  // rows per band - 1
+  const float J = a.f_J, dt = a.f_dt, dt4 = a.f_dt4;
+  const T rsl_s = make_float2(a.f_par[0], a.f_par[1]);
+  const T iU_s = make_float2(a.f_par[2], a.f_par[3]);
+  const T iF_s = make_float2(a.f_par[4], a.f_par[5]);
+  constexpr uint32_t TS = uint32_t(sizeof(T));
+  T* const own0 = reinterpret_cast<T*>(smem_raw);
+  T* const own1 = own0 + 2 * q;
+  const uint32_t oa0 = smem_addr(own0), oa1 = smem_addr(own1);
+  const uint32_t pa0 = cluster_addr(oa0, uint32_t(rank ^ 1)), pa1 = cluster_addr(oa1, uint32_t(rank ^ 1));
+  // slots of the peer's band edges: a band's first row looks up into the
+  // peer's last row (slot q - ny + c, in the peer's high band when the site's
+  // band index equals the rank), its last row down into the peer's first row
+  const uint32_t up_edge[2] = {uint32_t(q - ny + (rank == 0 ? q : 0)), uint32_t(q - ny + (rank == 1 ? q : 0))};
+  const uint32_t dn_edge[2] = {uint32_t(rank == 0 ? 0 : q), uint32_t(rank == 1 ? 0 : q)};
+  const int lo0 = rank * q;
+  const int t = threadIdx.x;
+  const int64_t nclusters = gridDim.x / 2;
+  for (int64_t tr = blockIdx.x / 2; tr < a.ntraj; tr += nclusters) {
+    T* st = reinterpret_cast<T*>(a.state) + tr * N;
+    const T* __restrict__ g_rsl = a.rsl ? reinterpret_cast<const T*>(a.rsl) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iU = !FAST && a.iU ? reinterpret_cast<const T*>(a.iU) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iF = !FAST && a.iF ? reinterpret_cast<const T*>(a.iF) + tr * a.par_stride : nullptr;
+    const uint32_t seed = a.seeds[tr], id = a.ids[tr];
+    const T* noise_tr = reinterpret_cast<const T*>(a.noise) + tr * a.noise_traj_stride;
+    for (int j = t; j < q; j += CTA) {
+      own0[j] = st[lo0 + j];
+      own0[q + j] = st[lo0 + j + half];
+    }
+    cl.sync();
+    int b = 0;
+    bool bad = false;
+    for (int64_t step = 0; step < a.nsteps; ++step) {
+      const uint32_t gstep = a.step0 + uint32_t(step);
+      const uint32_t cur = b ? oa1 : oa0, nxt = b ? oa0 : oa1, peer = b ? pa1 : pa0;
+#pragma unroll 1
+      for (int j = t; j < q; j += CTA) {
+        const int pl = lo0 + j;
+        const int c = j & m, rb = (j >> lny) & rb_last;
+        T xi_lo, xi_hi;
+        if (FAST || a.noise_mode == 0) {
+          const u32x4 w = wiener_words(uint32_t(pl), gstep, seed, id);
+          xi_lo = normal_pair(w.x, w.y, 0.0f);
+          xi_hi = normal_pair(w.z, w.w, 0.0f);
+        } else {
+          const T* nz = noise_tr + int64_t(gstep) * N;
+          xi_lo = nz[pl];
+          xi_hi = nz[pl + half];
+        }
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          const uint32_t sl = uint32_t(k * q + j);        // own slot of the site
+          const uint32_t row0 = sl - uint32_t(c);
+          const T right = lds_c(cur + (row0 + uint32_t((c + 1) & m)) * TS, T{});
+          const T left = lds_c(cur + (row0 + uint32_t((c - 1) & m)) * TS, T{});
+          const T down = rb == rb_last ? ldc_c(peer + (dn_edge[k] + uint32_t(c)) * TS, T{})
+                                       : lds_c(cur + (sl + uint32_t(ny)) * TS, T{});
+          const T up = rb == 0 ? ldc_c(peer + (up_edge[k] + uint32_t(c)) * TS, T{})
+                               : lds_c(cur + (sl - uint32_t(ny)) * TS, T{});
+          const T sv = cadd(cadd(right, left), cadd(down, up));
+          const T h = make_float2(J * sv.y, -J * sv.x);  // -i J s
+          const int p = k ? pl + half : pl;
+          const T rr = g_rsl ? __ldg(g_rsl + p) : rsl_s;
+          const T uu = !FAST && g_iU ? __ldg(g_iU + p) : iU_s;
+          const T ff = !FAST && g_iF ? __ldg(g_iF + p) : iF_s;
+          const T v = lds_c(cur + sl * TS, T{});
+          sts_c(nxt + sl * TS, local_update(v, h, rr, uu, ff, dt, dt4, k ? xi_hi : xi_lo));
+        }
+      }
+      b ^= 1;
+      cl.sync();
+    }
+    const T* fin = b ? own1 : own0;
+    for (int j = t; j < q; j += CTA) {
+      const T v0 = fin[j], v1 = fin[q + j];
+      st[lo0 + j] = v0;
+      st[lo0 + j + half] = v1;
+      bad |= !finite_c(v0) || !finite_c(v1);
+    }
+    set_status(a.status, tr, bad);
+    __syncthreads();  // the write-back reads buffer b before the next trajectory loads buffer 0
+  }
+}
+
+template <int CTA, bool FAST>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(CTA, 1) ell_cluster_pow2_kernel(const StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  ell_cluster_pow2_body<CTA, FAST>(a, smem_raw);
+}
+
+template <int CTA, bool FAST>
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(CTA, 1) ell_cluster_pow2_kernel_dev(const StepArgs* __restrict__ ap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) StepArgs s_a;
+  for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += CTA)
+    reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(ap)[i];
+  __syncthreads();
+  ell_cluster_pow2_body<CTA, FAST>(s_a, smem_raw);
+}
+
 }  // namespace twmc

@@ -36,16 +36,48 @@ def test_square_stencil_parity(built_lib, oracle, shape, prec):
     check(res, refs, prec)
 
 
-@pytest.mark.parametrize("shape", [(128, 128), (96, 128), (99, 101), (1, 16384)])
-def test_cluster_stencil_parity(built_lib, oracle, shape):
-    """Lattices above 8192 sites (FP32) run on the 2-CTA cluster kernel, the
+@pytest.mark.parametrize("shape,kernel", [((128, 128), "ell_cluster_pow2_kernel"), ((64, 256), "ell_cluster_pow2_kernel"),
+                                          ((256, 64), "ell_cluster_pow2_kernel"), ((4, 4096), "ell_cluster_pow2_kernel"),
+                                          ((96, 128), "ell_cluster_kernel"), ((99, 101), "ell_cluster_kernel"),
+                                          ((1, 16384), "ell_cluster_kernel")])
+def test_cluster_stencil_parity(built_lib, oracle, shape, kernel):
+    """Lattices above 8192 sites (FP32) run on a 2-CTA cluster kernel, the
     neighbours of the other CTA's quarters read through distributed shared
-    memory; odd N leaves the last pair without its high site."""
+    memory; odd N leaves the last pair without its high site. Power-of-two
+    lattices with every row inside one quarter (ny <= N / 4) take the
+    bit-arithmetic form (one row per quarter at 4 x 4096)."""
     nx, ny = shape
     res, refs = square_case(oracle, nx, ny, ntraj=3, prec=twmc.PREC_F32, hop=twmc.HOP_STENCIL, steps=60,
                             frame_steps=20)
-    assert res["kernel"] == "ell_cluster_kernel"
+    assert res["kernel"] == kernel
     check(res, refs, twmc.PREC_F32)
+
+
+@pytest.mark.parametrize("shape,site_omega", [((128, 128), False), ((128, 128), True), ((4, 4096), False),
+                                              ((256, 64), True)])
+def test_cluster_pow2_philox(built_lib, oracle, shape, site_omega):
+    """Philox-mode runs on the fast power-of-two cluster kernel (noise and
+    scalar U, F compiled in; omega per site allowed) against the oracle's
+    Philox stream (FP32 Box-Muller flavour)."""
+    nx, ny = shape
+    n = nx * ny
+    ntraj, steps, dt = 2, 100, 0.005
+    rng = np.random.default_rng(11)
+    beta0 = 0.3 * (rng.normal(size=(ntraj, n)) + 1j * rng.normal(size=(ntraj, n)))
+    omega = -0.5 + 0.2 * rng.normal(size=n) if site_omega else -0.5
+    sysd = twmc.System(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=dt, frame_steps=50, omega=omega, U=0.2, F=1.5,
+                       precision=twmc.PREC_F32, noise=twmc.NOISE_PHILOX, hop=twmc.HOP_STENCIL)
+    seeds = [21, 4242]
+    tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=steps * dt, ic=twmc.IC_GIVEN, init_field=beta0, seeds=seeds,
+                            id0=9)
+    res = sysd.run(tasks, frames=False)
+    kernel = sysd.kernel_name
+    sysd.close()
+    assert kernel == "ell_cluster_pow2_kernel"
+    for k in range(ntraj):
+        ref = oracle.base_run(nx, ny, 1.0, 1.0, dt, 0.0, steps * dt, 50, 3, True, omega, 0.2, 1.5, beta0[k],
+                              seed=seeds[k], tid=9 + k, noise="philox32")
+        assert rel_err(res["final"][k], ref["final"]) < 1e-4
 
 
 def test_cluster_per_site_parameters(built_lib, oracle):
@@ -55,7 +87,7 @@ def test_cluster_per_site_parameters(built_lib, oracle):
     F = 1.0 + 0.3 * rng.normal(size=n) + 0.1j
     res, refs = square_case(oracle, 128, 128, ntraj=2, prec=twmc.PREC_F32, hop=twmc.HOP_STENCIL, omega=omega, F=F,
                             steps=40, frame_steps=20)
-    assert res["kernel"] == "ell_cluster_kernel"
+    assert res["kernel"] == "ell_cluster_pow2_kernel"
     check(res, refs, twmc.PREC_F32)
 
 
