@@ -571,28 +571,55 @@ int download_real(twmc_handle* h, const DevBuf& b, double* out, size_t n) {
   return TWMC_OK;
 }
 
-// The batch's field as complex128 into host memory. FP32 state is widened on
-// the GPU in chunks of at most kWideChunk doubles (a bounded per-handle
-// buffer), each chunk copied straight to its place in `out`.
+// The batch's field as complex128 into host memory, trajectory r at
+// out + r * row_stride doubles (row_stride >= 2 N), enqueued on the handle's
+// stream without a final synchronisation: with a pinned destination the copy
+// overlaps whatever the caller enqueues next. FP32 state is widened on the
+// GPU in chunks of whole trajectories of at most kWideChunk doubles (a
+// bounded per-handle buffer), each chunk copied straight to its rows by one
+// strided copy.
 constexpr size_t kWideChunk = size_t(1) << 25;  // 256 MB of doubles
 
-int download_field(twmc_handle* h, double* out) {
-  const size_t n = size_t(h->ntraj * h->nsites);
+int download_rows(twmc_handle* h, double* out, size_t row_stride) {
+  const size_t rows = size_t(h->ntraj), row = size_t(2 * h->nsites);  // doubles per trajectory
+  if (rows == 0) return TWMC_OK;
+  int maxpitch = 0;
+  cudaDeviceGetAttribute(&maxpitch, cudaDevAttrMaxPitch, h->device);
+  const bool strided = row_stride * sizeof(double) <= size_t(maxpitch);
+  auto copy_rows = [&](double* dst, const void* src_rows, size_t m) -> cudaError_t {
+    if (row_stride == row)  // consecutive rows: one flat copy
+      return cudaMemcpyAsync(dst, src_rows, m * row * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+    if (strided)
+      return cudaMemcpy2DAsync(dst, row_stride * sizeof(double), src_rows, row * sizeof(double), row * sizeof(double), m,
+                               cudaMemcpyDeviceToHost, h->stream);
+    for (size_t r = 0; r < m; ++r) {  // pitch above the device limit: one copy per trajectory
+      const cudaError_t e = cudaMemcpyAsync(dst + r * row_stride, static_cast<const double*>(src_rows) + r * row,
+                                            row * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
+      if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+  };
   if (h->prec) {
-    TWMC_CUDA(h, cudaMemcpyAsync(out, h->d_state.p, n * 2 * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
-    TWMC_CUDA(h, cudaStreamSynchronize(h->stream));
+    TWMC_CUDA(h, copy_rows(out, h->d_state.p, rows));
     return TWMC_OK;
   }
-  const size_t total = 2 * n;
-  const size_t chunk = std::min(total, kWideChunk);
-  if (!h->d_wide.ensure(chunk * sizeof(double))) return fail(h, TWMC_ERR_NOMEM, "download buffer allocation");
+  const size_t per = std::max<size_t>(1, std::min(rows, kWideChunk / row));  // trajectories per chunk
+  if (!h->d_wide.ensure(per * row * sizeof(double))) return fail(h, TWMC_ERR_NOMEM, "download buffer allocation");
   const float* src = static_cast<const float*>(h->d_state.p);
-  for (size_t off = 0; off < total; off += chunk) {
-    const size_t m = std::min(chunk, total - off);
+  for (size_t r0 = 0; r0 < rows; r0 += per) {
+    const size_t m = std::min(per, rows - r0);
     std::string err;
-    if (!widen_launch(src + off, h->d_wide.as<double>(), int64_t(m), h->stream, &err)) return fail(h, TWMC_ERR_CUDA, err);
-    TWMC_CUDA(h, cudaMemcpyAsync(out + off, h->d_wide.p, m * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (!widen_launch(src + r0 * row, h->d_wide.as<double>(), int64_t(m * row), h->stream, &err))
+      return fail(h, TWMC_ERR_CUDA, err);
+    TWMC_CUDA(h, copy_rows(out + r0 * row_stride, h->d_wide.p, m));
   }
+  return TWMC_OK;
+}
+
+// The batch's field as contiguous complex128 rows; returns after the copy.
+int download_field(twmc_handle* h, double* out) {
+  int rc = download_rows(h, out, size_t(2 * h->nsites));
+  if (rc) return rc;
   TWMC_CUDA(h, cudaStreamSynchronize(h->stream));
   return TWMC_OK;
 }
@@ -859,21 +886,35 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
           std::memcpy(real_dst[m] + idx[i] * N * 2, &tmp[i * N * 2], sizeof(double) * size_t(N * 2));
       }
       std::vector<double> fbuf;
+      // tasks of this group in consecutive output rows: frames and the final
+      // field are copied to their places by strided asynchronous copies
+      bool contiguous = true;
+      for (size_t i = 1; i < bn && contiguous; ++i) contiguous = idx[i] == idx[0] + i;
       auto save_frame = [&](int64_t f) -> int {
         if (out && out->moments) {
           int r2 = reduce(h);
           if (r2) return r2;
-          std::vector<double> mb(size_t(nb) * N * 3, 0.0);
-          r2 = twmc_batch_download(h, nullptr, mb.data());
-          if (r2) return r2;
-          std::memcpy(out->moments + size_t(f) * nb * N * 3, mb.data(), mb.size() * sizeof(double));
+          double* dst = out->moments + size_t(f) * nb * N * 3;
+          if (int64_t(bn) >= nb) {  // every block holds trajectories: one copy, no wait
+            TWMC_CUDA(h, cudaMemcpyAsync(dst, h->d_moments.p, size_t(nb) * N * 3 * sizeof(double),
+                                         cudaMemcpyDeviceToHost, h->stream));
+          } else {
+            r2 = twmc_batch_download(h, nullptr, dst);
+            if (r2) return r2;
+          }
         }
         if (out && out->frames) {
-          fbuf.resize(size_t(bn * N * 2));
-          int r2 = download_field(h, fbuf.data());
-          if (r2) return r2;
-          for (size_t i = 0; i < bn; ++i)
-            std::memcpy(out->frames + (idx[i] * max_frames + f) * N * 2, &fbuf[i * N * 2], sizeof(double) * size_t(N * 2));
+          if (contiguous) {
+            int r2 = download_rows(h, out->frames + (idx[0] * max_frames + f) * N * 2, size_t(max_frames * N * 2));
+            if (r2) return r2;
+          } else {
+            fbuf.resize(size_t(bn * N * 2));
+            int r2 = download_field(h, fbuf.data());
+            if (r2) return r2;
+            for (size_t i = 0; i < bn; ++i)
+              std::memcpy(out->frames + (idx[i] * max_frames + f) * N * 2, &fbuf[i * N * 2],
+                          sizeof(double) * size_t(N * 2));
+          }
         }
         if (h->thermo) {  // work / area since the previous save, then reset
           double* dst[2] = {out ? out->work : nullptr, out ? out->area : nullptr};
@@ -912,12 +953,9 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
         if (rc) return rc;
         done_steps += (s.steps - cur) * int64_t(bn);
       }
-      TWMC_CUDA(h, cudaStreamSynchronize(h->stream));
       if (out && out->final_field) {
-        bool contiguous = true;  // tasks of this group in consecutive output rows: download in place
-        for (size_t i = 1; i < bn && contiguous; ++i) contiguous = idx[i] == idx[0] + i;
         if (contiguous) {
-          rc = download_field(h, out->final_field + idx[0] * N * 2);
+          rc = download_rows(h, out->final_field + idx[0] * N * 2, size_t(N * 2));
           if (rc) return rc;
         } else {
           fbuf.resize(size_t(bn * N * 2));
@@ -928,7 +966,8 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
         }
       }
       std::vector<int> st(bn);
-      TWMC_CUDA(h, cudaMemcpy(st.data(), h->d_status.p, bn * sizeof(int), cudaMemcpyDeviceToHost));
+      TWMC_CUDA(h, cudaMemcpyAsync(st.data(), h->d_status.p, bn * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
+      TWMC_CUDA(h, cudaStreamSynchronize(h->stream));
       for (size_t i = 0; i < bn; ++i) {
         if (out && out->status) out->status[idx[i]] = st[i];
         if (out && out->t_final) out->t_final[idx[i]] = s.t_final;

@@ -106,6 +106,31 @@ def test_moments_match_frames(built_lib, oracle):
             assert np.allclose(res["moments"][f, b, :, 2], (np.abs(fk) ** 2).sum(0), rtol=1e-10, atol=1e-10)
 
 
+def test_fp32_moments_float_float(built_lib):
+    """FP32 states: the float-float block sums equal FP64 sums of the
+    downloaded (exactly widened) fields to 1e-12 relative, over amplitudes
+    spread across seven decades and with one site whose |a|^2 >= 2^60 takes
+    the FP64 branch."""
+    nx = ny = 8
+    n = nx * ny
+    ntraj, nb = 300, 3
+    rng = np.random.default_rng(4)
+    b0 = (rng.normal(size=(ntraj, n)) + 1j * rng.normal(size=(ntraj, n))) * np.exp(rng.uniform(-8, 8, (ntraj, n)))
+    b0[5, 3] = 3e9 + 1e9j
+    sysd = twmc.System(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=0.005, frame_steps=1, omega=-0.5, U=0.0, F=0.0,
+                       precision=twmc.PREC_F32, n_moment_blocks=nb, hop=twmc.HOP_STENCIL)
+    tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=0.005, ic=twmc.IC_GIVEN, init_field=b0)
+    res = sysd.run(tasks, frames=True, moments=True)
+    sysd.close()
+    x = res["frames"][:, 0]
+    assert np.array_equal(x, b0.astype(np.complex64).astype(np.complex128))
+    for b in range(nb):
+        t0, t1 = b * ntraj // nb, (b + 1) * ntraj // nb
+        ab2 = x[t0:t1].real ** 2 + x[t0:t1].imag ** 2
+        assert np.allclose(res["moments"][0, b, :, 0], ab2.sum(0), rtol=1e-12, atol=0)
+        assert np.allclose(res["moments"][0, b, :, 1], (ab2 ** 2).sum(0), rtol=1e-12, atol=0)
+
+
 def test_nonfinite_status_flag(built_lib):
     """A NaN injected into one trajectory's host noise is reported in its status only."""
     nx = ny = 16
@@ -162,6 +187,34 @@ def test_full_size_fft_equals_stencil(built_lib):
     assert np.isfinite(fa).all()
     assert rel_err(fa, fb) < 1e-4
     assert np.allclose(ma[:, :, 0].sum(0), (np.abs(fa) ** 2).sum(0), rtol=1e-9)
+
+
+def test_run_interleaved_groups_and_pinned_buffers(built_lib):
+    """Tasks of two horizons interleaved in one call form two groups whose
+    output rows are not consecutive (the copy-through-host path); each group
+    equals a call of its tasks alone (consecutive rows: strided asynchronous
+    copies), into pageable and into pinned result arrays alike."""
+    import torch
+    s = twmc.System(nx=16, ny=16, J=1.0, gamma=1.0, dt=0.002, frame_steps=25,
+                    omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=0.2, F=1.5, beta_init_sigma=0.5)
+    tasks = s.make_tasks(40, t_end=0.1, seed0=3, store_initial=True)
+    for k in range(1, 40, 2):
+        tasks[k].t_end = 0.05
+    both = s.run(tasks, frames=True, final=True, moments=False)
+    for sel, nf in ((slice(0, 40, 2), 3), (slice(1, 40, 2), 2)):
+        sub = s.make_tasks(20, t_end=0.1, seed0=3, store_initial=True)
+        for j, k in enumerate(range(40)[sel]):
+            sub[j].seed, sub[j].id, sub[j].t_end = tasks[k].seed, tasks[k].id, tasks[k].t_end
+        alone = s.run(sub, frames=True, final=True)
+        assert alone["frames"].shape == (20, nf, 256)
+        assert np.array_equal(both["final"][sel], alone["final"])
+        assert np.array_equal(both["frames"][sel, :nf], alone["frames"])
+        pinned = {"final": torch.empty((20, 256), dtype=torch.complex128, pin_memory=True).numpy(),
+                  "frames": torch.empty((20, nf, 256), dtype=torch.complex128, pin_memory=True).numpy()}
+        got = s.run(sub, frames=True, final=True, buffers=pinned)
+        assert np.array_equal(got["final"], alone["final"])
+        assert np.array_equal(got["frames"], alone["frames"])
+    s.close()
 
 
 def test_run_into_caller_buffers(built_lib):
