@@ -46,6 +46,14 @@ __device__ __forceinline__ double2 lds_c(uint32_t a, double2) {
   asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(a) : "memory");
   return v;
 }
+// Four consecutive reals from shared memory (16-byte aligned for FP32).
+__device__ __forceinline__ void lds_r4(uint32_t a, float* w) {
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(w[0]), "=f"(w[1]), "=f"(w[2]), "=f"(w[3]) : "r"(a) : "memory");
+}
+__device__ __forceinline__ void lds_r4(uint32_t a, double* w) {
+  asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(w[0]), "=d"(w[1]) : "r"(a) : "memory");
+  asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(w[2]), "=d"(w[3]) : "r"(a + 16u) : "memory");
+}
 __device__ __forceinline__ void sts_c(uint32_t a, float2 v) {
   asm volatile("st.shared.v2.f32 [%0], {%1, %2};" ::"r"(a), "f"(v.x), "f"(v.y) : "memory");
 }

@@ -28,9 +28,10 @@ bool ell_launch_t(const StepArgs& a0, cudaStream_t s, LaunchInfo* info, std::str
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   int maxsm = 0;
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  size_t smem = sizeof(T) * size_t(2) * tpc * size_t(a.nsites);
+  const size_t wbytes = HOP == 0 ? size_t(a.nsites) * 4 * sizeof(R) : 0;  // Lieb weights
   a.dbuf = 1;
-  if (smem > size_t(maxsm)) { smem /= 2; a.dbuf = 0; }
+  size_t smem = ell_state_bytes(true, tpc, a.nsites, sizeof(T)) + wbytes;
+  if (smem > size_t(maxsm)) { a.dbuf = 0; smem = ell_state_bytes(false, tpc, a.nsites, sizeof(T)) + wbytes; }
   if (smem > size_t(maxsm)) { if (err) *err = "ell kernel: trajectory does not fit in shared memory"; return false; }
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) { cudaGetLastError(); if (err) *err = std::string("ell smem: ") + cudaGetErrorString(e); return false; }
@@ -93,9 +94,10 @@ bool ell_prep_t(StepArgs* a, int* grid, size_t* smem_out, std::string* err) {
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const int avail = maxsm - int(sizeof(StepArgs)) - 64;
-  size_t smem = sizeof(T) * size_t(2) * tpc * size_t(a->nsites);
+  const size_t wbytes = HOP == 0 ? size_t(a->nsites) * 4 * sizeof(R) : 0;  // Lieb weights
   a->dbuf = 1;
-  if (smem > size_t(avail)) { smem /= 2; a->dbuf = 0; }
+  size_t smem = ell_state_bytes(true, tpc, a->nsites, sizeof(T)) + wbytes;
+  if (smem > size_t(avail)) { a->dbuf = 0; smem = ell_state_bytes(false, tpc, a->nsites, sizeof(T)) + wbytes; }
   if (smem > size_t(avail)) { if (err) *err = "ell kernel: trajectory does not fit in shared memory"; return false; }
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) { cudaGetLastError(); if (err) *err = std::string("ell smem: ") + cudaGetErrorString(e); return false; }

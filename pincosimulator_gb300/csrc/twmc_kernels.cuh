@@ -506,7 +506,10 @@ __global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel
 // two sites of one Philox call live in the same thread. Site indices are
 // recomputed from t (one multiply-add), not stored.
 // HOP = 0: neighbour table h = sum_j w_pj b[idx_pj] (Lieb couplings), the
-//          indices kept in registers as packed 16-bit pairs (N <= 16384).
+//          indices kept in registers as packed 16-bit pairs (N <= 16384),
+//          the weights -- purely imaginary (-i J), as the host builds them --
+//          as their imaginary parts in shared memory behind the field
+//          buffers, four per site in one 16-byte row (FP32).
 // HOP = 1: square stencil h = -i J (wy (b[c+1] + b[c-1]) + wx (b[r+1] + b[r-1])),
 //          the (row, column) of each site advanced incrementally through the
 //          thread's sites every step, so nothing per site but the field is
@@ -514,6 +517,12 @@ __global__ void __launch_bounds__(CTA, sizeof(R) == 4 ? 2 : 1) square_fft_kernel
 // FAST: the common run (Philox noise, no F(t), no work / area) with those
 //       features compiled out instead of tested per site.
 // ------------------------------------------------------------------------
+// Bytes of the real-space kernel's field buffers (one or two per trajectory
+// slot), rounded up to 16 so that the Lieb weights behind them start aligned.
+__host__ __device__ __forceinline__ size_t ell_state_bytes(bool dbuf, int tpc, int64_t n, size_t csize) {
+  return ((dbuf ? 2 : 1) * size_t(tpc) * size_t(n) * csize + 15) & ~size_t(15);
+}
+
 template <typename R, int VPT, int CTA, int HOP, bool FAST = false>
 __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_raw) {
   using T = c2_t<R>;
@@ -552,6 +561,13 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
     dr = tpt / ny; dc = tpt % ny;
   }
   const T* __restrict__ g_w = reinterpret_cast<const T*>(a.nbr_w);
+  uint32_t swa = 0;  // shared-memory address of the weights (HOP = 0)
+  if constexpr (HOP == 0) {
+    const size_t sbytes = ell_state_bytes(a.dbuf != 0, tpc, N, sizeof(T));
+    R* s_wt = reinterpret_cast<R*>(smem_raw + sbytes);
+    for (int i = tid; i < 4 * N; i += CTA) s_wt[i] = g_w[i].y;  // covered by the first step's barrier
+    swa = smem_addr(s_wt);
+  }
   const R wy = ny > 1 ? R(1) : R(0), wx = nx > 1 ? R(1) : R(0);
   constexpr bool F32 = sizeof(R) == 4;
   const R J = F32 ? R(a.f_J) : R(a.J);
@@ -590,11 +606,14 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
       auto hop_table = [&](int v) -> T {
         const T b0 = ld_site(int(nb01[HOP == 0 ? v : 0] & 0xFFFFu)), b1 = ld_site(int(nb01[HOP == 0 ? v : 0] >> 16));
         const T b2 = ld_site(int(nb23[HOP == 0 ? v : 0] & 0xFFFFu)), b3 = ld_site(int(nb23[HOP == 0 ? v : 0] >> 16));
-        const T* w = g_w + int64_t(site_of(v)) * 4;
-        T acc = cmul(__ldg(w), b0);
-        acc = cadd(acc, cmul(__ldg(w + 1), b1));
-        acc = cadd(acc, cmul(__ldg(w + 2), b2));
-        return cadd(acc, cmul(__ldg(w + 3), b3));
+        R w[4];  // idle slots read site 0's row, as their neighbour indices do
+        lds_r4(swa + uint32_t(valid_of(v) ? site_of(v) : 0) * uint32_t(4 * sizeof(R)), w);
+        // (i w) b with each product rounded once, as the complex product with
+        // a zero real part gives
+        T acc = cmake<T>(-(w[0] * b0.y), w[0] * b0.x);
+        acc = cadd(acc, cmake<T>(-(w[1] * b1.y), w[1] * b1.x));
+        acc = cadd(acc, cmake<T>(-(w[2] * b2.y), w[2] * b2.x));
+        return cadd(acc, cmake<T>(-(w[3] * b3.y), w[3] * b3.x));
       };
       auto hop_stencil = [&](int p, int r, int c) -> T {
         const int right = c + 1 < ny ? p + 1 : p + 1 - ny, left = c > 0 ? p - 1 : p - 1 + ny;
