@@ -101,12 +101,12 @@ def measured_peaks():
         return {}
 
 
-def _profile_figure(key):
-    """A figure `key: <number>` from the committed ncu summary of the step
-    kernel (profiles/square_fft_kernel_64x64.md), or None."""
+def _profile_figure(key, profile="square_fft_kernel_64x64.md"):
+    """A figure `key: <number>` from a committed ncu summary of a step kernel
+    (default: the FFT kernel on the headline workload), or None."""
     import re
     try:
-        txt = open(os.path.join(ROOT, "profiles", "square_fft_kernel_64x64.md")).read()
+        txt = open(os.path.join(ROOT, "profiles", profile)).read()
     except OSError:
         return None
     m = re.search(re.escape(key) + r":\s*([0-9.eE+]+)", txt)
@@ -136,7 +136,7 @@ def make_system(twmc, hop=None, precision=None):
                        hop=twmc.HOP_FFT if hop is None else hop, n_moment_blocks=32)
 
 
-def measure_other_paths(twmc, torch):
+def measure_other_paths(twmc, torch, sm_mhz=None):
     """Throughput of the other configurations, one timed unit each: the
     headline workload on the real-space stencil kernel (the same hopping
     operator applied without the FFT), the 256-point heterogeneous batch
@@ -160,6 +160,14 @@ def measure_other_paths(twmc, torch):
     ms = e0.elapsed_time(e1) / 2
     out["headline_real_space"] = {"value": FRAME_STEPS * NTRAJ * NX * NY / (ms / 1e3), "unit": METRIC,
                                   "kernel": sysd.kernel_name, "ms_per_frame": ms}
+    ipsu = _profile_figure("inst_per_site_update", "ell_kernel_64x64_stencil.md")
+    if ipsu and sm_mhz:
+        sms = torch.cuda.get_device_properties(0).multi_processor_count
+        ach = out["headline_real_space"]["value"] * ipsu / 32.0
+        out["headline_real_space"]["issue"] = {
+            "inst_per_site_update": ipsu, "frac": ach / (sms * 4 * sm_mhz * 1e6),
+            "source": "ncu instruction count (profiles/ell_kernel_64x64_stencil.md) x measured rate; "
+                      "peak = SMs x 4 schedulers x median SM clock of the headline run"}
     sysd.close()
     rng = np.random.default_rng(3)
     kinds = [(1, n) for n in (32, 64, 128, 256, 512, 1024)] + [(l, l) for l in (16, 32, 64, 128)]
@@ -408,7 +416,7 @@ def main():
         f64["fp32_speedup"] = value / f64["value"]
     other = None
     if world == 1 and args.ntraj == NTRAJ and not args.no_other:
-        other = measure_other_paths(twmc, torch)
+        other = measure_other_paths(twmc, torch, clocks.get("sm_mhz") if clocks else None)
     hbm = peaks.get("hbm_gbs")
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
