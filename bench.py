@@ -379,16 +379,18 @@ def main():
                                        pin_memory=True).numpy()}
         sysd.run(tasks, frames=False, final=True, moments=True, buffers=bufs)
         reps = 2
-        t0 = time.perf_counter()
+        calls = []
         for _ in range(reps):
+            t0 = time.perf_counter()
             res = sysd.run(tasks, frames=False, final=True, moments=True, buffers=bufs)
-        el = (time.perf_counter() - t0) / reps
+            calls.append(time.perf_counter() - t0)
+        el = sum(calls) / reps
         sysd.close()
         n_fr = args.e2e_steps
         h2d = (NTRAJ * (8 + 8) + 5 * 2 * NX * NY * 16) / n_fr
         d2h = (res["final"].size * 8 + n_fr * 32 * NX * NY * 3 * 8 + NTRAJ * (8 + 8 + 4)) / n_fr
         e2e = {"value": n_fr * FRAME_STEPS * NTRAJ * NX * NY / el, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "api": "twmc_run (pinned host result buffers reused across calls: "
+               "d2h_bytes_per_step": int(d2h), "calls_ms": [round(c * 1e3, 2) for c in calls], "api": "twmc_run (pinned host result buffers reused across calls: "
                "final field widened to complex128 on the GPU, FP64 moment blocks every frame; initial draws and "
                "disorder on the GPU inside the call; mean of 2 calls after 1 warm-up)"}
         del res

@@ -32,9 +32,9 @@ def _setup(lib):
                                    C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p]
     lib.orc_time_table_eval.argtypes = [C.c_void_p, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p, C.c_int64,
                                         C.c_void_p]
-    lib.orc_initial_field.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p]
+    lib.orc_initial_field.argtypes = [C.c_int64, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_int]
     lib.orc_disorder.argtypes = [C.c_int64, C.c_int, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint32,
-                                 C.c_void_p]
+                                 C.c_void_p, C.c_int]
     lib.orc_base_run_batch.argtypes = [C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double,
                                        C.c_double, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
                                        C.c_void_p, C.c_int64, C.c_uint32, C.c_int, C.c_void_p]
@@ -164,15 +164,15 @@ def time_table_eval(times, vals, ts):
     return out
 
 
-def initial_field(n, binit, bsigma, seed, tid):
+def initial_field(n, binit, bsigma, seed, tid, f32=False):
     bi, bs = _c(np.broadcast_to(binit, (n,))), _c(np.broadcast_to(bsigma, (n,)))
     out = np.zeros(n, dtype=np.complex128)
-    load().orc_initial_field(n, bi.ctypes.data, bs.ctypes.data, seed, tid, out.ctypes.data)
+    load().orc_initial_field(n, bi.ctypes.data, bs.ctypes.data, seed, tid, out.ctypes.data, int(f32))
     return out
 
 
-def disorder(n, kind, base, amp, seed, tid, stream):
+def disorder(n, kind, base, amp, seed, tid, stream, f32=False):
     b, a = _c(np.broadcast_to(base, (n,))), _c(np.broadcast_to(amp, (n,)))
     out = np.zeros(n, dtype=np.complex128)
-    load().orc_disorder(n, kind, b.ctypes.data, a.ctypes.data, seed, tid, stream, out.ctypes.data)
+    load().orc_disorder(n, kind, b.ctypes.data, a.ctypes.data, seed, tid, stream, out.ctypes.data, int(f32))
     return out

@@ -542,26 +542,29 @@ void orc_time_table_eval(const double* times, const double* vals_ri, int64_t nre
 // Initial field as TWMCBaseSolver::Compute forms it for ReadFromSettings
 // (:126-135): beta = beta_init + beta_init_sigma (*) xi, xi from the
 // initial-condition stream, FP64 flavour.
+// f32_flavour: the Box-Muller flavour of FP32 runs (as for the Wiener noise);
+// the combination with beta_init / beta_init_sigma stays in FP64.
 void orc_initial_field(int64_t n, const double* binit_ri, const double* bsigma_ri, uint32_t seed, uint32_t tid,
-                       double* out_ri) {
+                       double* out_ri, int f32_flavour) {
   const cd* bi = reinterpret_cast<const cd*>(binit_ri);
   const cd* bs = reinterpret_cast<const cd*>(bsigma_ri);
   cd* out = reinterpret_cast<cd*>(out_ri);
-  for (int64_t p = 0; p < n; ++p) out[p] = bi[p] + bs[p] * site_normal(seed, tid, 0, kStreamInit, p, n, 0);
+  for (int64_t p = 0; p < n; ++p)
+    out[p] = bi[p] + bs[p] * site_normal(seed, tid, 0, kStreamInit, p, n, f32_flavour);
 }
 
 // Disorder draw of NoisyMatrix::EvaluateNoise (NoisyMatrix.cpp:131-162) on a
 // Philox stream: kind 1 = Gaussian (re/im normals scaled by Re/Im of amp),
 // kind 2 = Uniform on [0,1) (u = w 2^-32 from words (0,1) / (2,3)).
 void orc_disorder(int64_t n, int kind, const double* base_ri, const double* amp_ri, uint32_t seed, uint32_t tid,
-                  uint32_t stream, double* out_ri) {
+                  uint32_t stream, double* out_ri, int f32_flavour) {
   const cd* base = reinterpret_cast<const cd*>(base_ri);
   const cd* amp = reinterpret_cast<const cd*>(amp_ri);
   cd* out = reinterpret_cast<cd*>(out_ri);
   for (int64_t p = 0; p < n; ++p) {
     cd nz(0, 0);
     if (kind == 1) {
-      cd z = site_normal(seed, tid, 0, stream, p, n, 0);
+      cd z = site_normal(seed, tid, 0, stream, p, n, f32_flavour);
       nz = cd(z.real() * amp[p].real(), z.imag() * amp[p].imag());
     } else if (kind == 2) {
       uint32_t c0; int lane;

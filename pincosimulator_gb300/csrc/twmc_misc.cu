@@ -14,6 +14,17 @@ __device__ __forceinline__ double2 ld_c(const double* p, int64_t i) { return mak
 
 // One trajectory-site of the initial state (TWMCBaseSolver.cpp:126-151 /
 // TWMCLiebSolver.cpp:145-171 with the noise drawn from Philox streams).
+// FP32 runs draw the normals with the FP32 Box-Muller of the Wiener noise,
+// FP64 runs with the FP64 one; the sums with the base values are FP64 in
+// both. (The FP64 logarithm and sine / cosine of two draws per site took
+// 20 ms for 16384 trajectories of 64 x 64 on GB300's narrow FP64 pipe.)
+__device__ __forceinline__ double2 init_normal(uint32_t a, uint32_t b, int prec) {
+  if (prec == 0) {
+    const float2 z = normal_pair(a, b, 0.0f);
+    return make_double2(double(z.x), double(z.y));
+  }
+  return normal_pair(a, b, 0.0);
+}
 __global__ void init_kernel(const InitArgs a) {
   const int64_t total = a.ntraj * a.nsites;
   for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
@@ -28,7 +39,7 @@ __global__ void init_kernel(const InitArgs a) {
       b = a.binit ? ld_c(a.binit, p) : make_double2(a.binit_s[0], a.binit_s[1]);
       if (a.ic_kind == 0) {
         const u32x4 w = philox4x32_10(u32x4{c0, 0u, kStreamInit, 0u}, seed, id);
-        const double2 z = hi ? normal_pair(w.z, w.w, 0.0) : normal_pair(w.x, w.y, 0.0);
+        const double2 z = hi ? init_normal(w.z, w.w, a.prec) : init_normal(w.x, w.y, a.prec);
         const double2 sg = a.bsigma ? ld_c(a.bsigma, p) : make_double2(a.bsigma_s[0], a.bsigma_s[1]);
         b = cadd(b, cmul(sg, z));
       }
@@ -45,7 +56,7 @@ __global__ void init_kernel(const InitArgs a) {
         const u32x4 w = philox4x32_10(u32x4{c0, 0u, a.stream[m], 0u}, seed, id);
         const double2 amp = ld_c(a.amp[m], p);
         if (a.kind[m] == 1) {
-          const double2 z = hi ? normal_pair(w.z, w.w, 0.0) : normal_pair(w.x, w.y, 0.0);
+          const double2 z = hi ? init_normal(w.z, w.w, a.prec) : init_normal(w.x, w.y, a.prec);
           v[m].x += z.x * amp.x;
           v[m].y += z.y * amp.y;
         } else {

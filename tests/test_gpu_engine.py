@@ -40,8 +40,12 @@ def test_philox_noise_trajectories(built_lib, oracle, prec, noise, tol, shape, h
         assert rel_err(res["final"][k], ref["final"]) < tol
 
 
-def test_initial_fields_and_disorder(built_lib, oracle):
-    """ReadFromSettings initial fields and Gaussian / Uniform disorder draws (FP64 state)."""
+@pytest.mark.parametrize("prec,tol", [(twmc.PREC_F64, 1e-14), (twmc.PREC_F32, 1e-5)])
+def test_initial_fields_and_disorder(built_lib, oracle, prec, tol):
+    """ReadFromSettings initial fields and Gaussian / Uniform disorder draws:
+    FP64 runs with the FP64 Box-Muller flavour (to 1e-14), FP32 runs with the
+    FP32 one (hardware logarithm and sine / cosine: 1e-5; the initial field
+    is then rounded to the FP32 state). Uniform draws are exact in both."""
     nx, ny, ntraj = 8, 8, 4
     n = nx * ny
     rng = np.random.default_rng(8)
@@ -54,16 +58,19 @@ def test_initial_fields_and_disorder(built_lib, oracle):
                        omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, om_amp),
                        U=twmc.Noisy(0.27, twmc.DISORDER_UNIFORM, u_amp),
                        F=twmc.Noisy(2.0, twmc.DISORDER_GAUSSIAN, f_amp),
-                       beta_init=binit, beta_init_sigma=bsig, precision=twmc.PREC_F64)
+                       beta_init=binit, beta_init_sigma=bsig, precision=prec)
     tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=0.01, seed0=77, id0=3)
     res = sysd.run(tasks, frames=True, realizations=True)
     sysd.close()
+    f32 = prec == twmc.PREC_F32
     for k in range(ntraj):
         seed, tid = 77 + k, 3 + k
-        assert rel_err(res["frames"][k, 0], oracle.initial_field(n, binit, bsig, seed, tid)) < 1e-14
-        assert rel_err(res["U_realization"][k], oracle.disorder(n, 2, 0.27, u_amp, seed, tid, 2)) < 1e-14
-        assert rel_err(res["omega_realization"][k], oracle.disorder(n, 1, -0.5, om_amp, seed, tid, 3)) < 1e-14
-        assert rel_err(res["F_realization"][k], oracle.disorder(n, 1, 2.0, f_amp, seed, tid, 4)) < 1e-14
+        assert rel_err(res["frames"][k, 0], oracle.initial_field(n, binit, bsig, seed, tid, f32=f32)) < tol
+        assert rel_err(res["U_realization"][k], oracle.disorder(n, 2, 0.27, u_amp, seed, tid, 2, f32=f32)) < 1e-14
+        assert rel_err(res["omega_realization"][k], oracle.disorder(n, 1, -0.5, om_amp, seed, tid, 3, f32=f32)) < tol
+        assert rel_err(res["F_realization"][k], oracle.disorder(n, 1, 2.0, f_amp, seed, tid, 4, f32=f32)) < tol
+    if f32:  # the FP32 flavour differs from the FP64 one by more than FP64 rounding
+        assert rel_err(res["omega_realization"][0], oracle.disorder(n, 1, -0.5, om_amp, 77, 3, 3)) > 1e-12
 
 
 def test_disordered_trajectories_match_oracle(built_lib, oracle):
