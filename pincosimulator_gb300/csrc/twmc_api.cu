@@ -95,6 +95,12 @@ struct twmc_handle {
   bool thermo = false;     // work / area accumulators (TWMCThermoSolver)
   DevBuf d_work, d_area;
   DevBuf d_wide;           // FP32 -> FP64 download staging (bounded chunk)
+  // final-field pipeline of twmc_run: the last steps run in kFinalChunks
+  // trajectory ranges; each range is widened into d_snap and copied to the
+  // host on dl_stream while the next range computes
+  cudaStream_t dl_stream = nullptr;
+  std::vector<cudaEvent_t> dl_ev;
+  DevBuf d_snap;
   std::vector<double> ft_times;   // with sentinel
   std::vector<cd> ft_vals, ft_slopes;
   // kernel selection
@@ -370,16 +376,25 @@ std::pair<cudaEvent_t, cudaEvent_t> get_events(twmc_handle* h) {
 }
 
 // Advances the batch by n steps (n may be 0 to refresh the k-space buffer).
-int advance(twmc_handle* h, int64_t n, bool want_nk) {
-  if (h->ntraj == 0) return TWMC_OK;
+// n steps of trajectories [t0, t1) of the batch (all when t1 < 0); the
+// step counter advances only when `bump` (a caller stepping the batch in
+// several ranges bumps it once).
+int advance(twmc_handle* h, int64_t n, bool want_nk, int64_t t0 = 0, int64_t t1 = -1, bool bump = true) {
+  if (t1 < 0) t1 = h->ntraj;
+  if (t1 <= t0) return TWMC_OK;
+  const size_t c2 = 2 * rsize(h->prec), r1 = rsize(h->prec);
+  const size_t row_c = size_t(h->nsites) * c2, row_r = size_t(h->nsites) * r1;  // bytes per trajectory
+  auto at = [&](const void* base, size_t row) -> void* {
+    return base ? static_cast<void*>(static_cast<char*>(const_cast<void*>(base)) + size_t(t0) * row) : nullptr;
+  };
   StepArgs a;
   std::memset(&a, 0, sizeof(a));
-  a.state = h->d_state.p;
-  a.ntraj = h->ntraj;
+  a.state = at(h->d_state.p, row_c);
+  a.ntraj = t1 - t0;
   a.nsteps = n;
   a.step0 = h->step_pos;
-  a.seeds = h->d_seeds.as<uint32_t>();
-  a.ids = h->d_ids.as<uint32_t>();
+  a.seeds = h->d_seeds.as<uint32_t>() + t0;
+  a.ids = h->d_ids.as<uint32_t>() + t0;
   const void** par[3] = {&a.rsl, &a.iU, &a.iF};
   double* sc[3] = {a.rsl_s, a.iU_s, a.iF_s};
   bool any_traj = false;
@@ -394,16 +409,17 @@ int advance(twmc_handle* h, int64_t n, bool want_nk) {
   // kinds are stored per trajectory in d_par when any is per trajectory)
   a.par_stride = any_traj ? h->nsites : 0;
   if (any_traj) for (int k = 0; k < 3; ++k) if (h->par_shared[k]) *par[k] = h->d_par[k].p;
+  if (any_traj) for (int k = 0; k < 3; ++k) *par[k] = at(*par[k], row_c);
   a.dt = h->dt;
   a.dt4 = std::sqrt(h->gamma * h->dt / 4.0);
   for (int k = 0; k < 3; ++k) { a.f_par[2 * k] = float(sc[k][0]); a.f_par[2 * k + 1] = float(sc[k][1]); }
   a.f_dt = float(a.dt);
   a.f_dt4 = float(a.dt4);
   a.noise_mode = h->noise_mode;
-  a.noise = h->d_noise.p;
   a.noise_traj_stride = h->noise_steps * h->nsites;
-  a.nk = (want_nk && h->use_fft) ? h->d_nk.p : nullptr;
-  a.status = h->d_status.as<int>();
+  a.noise = at(h->d_noise.p, size_t(a.noise_traj_stride) * c2);
+  a.nk = (want_nk && h->use_fft) ? at(h->d_nk.p, row_r) : nullptr;
+  a.status = h->d_status.as<int>() + t0;
   a.tw = h->d_tw.p;
   a.ktab = h->d_ktab.p;
   a.nsites = h->nsites;
@@ -421,8 +437,8 @@ int advance(twmc_handle* h, int64_t n, bool want_nk) {
     a.ft_dt = h->d_ft_dt.as<double>();
   }
   if (h->thermo) {
-    a.work = h->d_work.p;
-    a.area = h->d_area.p;
+    a.work = at(h->d_work.p, row_r);
+    a.area = at(h->d_area.p, row_r);
   }
   if (h->noise_mode == TWMC_NOISE_BUFFER && n > 0 && int64_t(h->step_pos) + n > h->noise_steps)
     return fail(h, TWMC_ERR_INVALID, "noise buffer shorter than the run");
@@ -443,7 +459,7 @@ int advance(twmc_handle* h, int64_t n, bool want_nk) {
   h->ev_pending.push_back(ev);
   if (!ok) return fail(h, TWMC_ERR_CUDA, err);
   ++h->launches;
-  h->step_pos += uint32_t(n);
+  if (bump) h->step_pos += uint32_t(n);
   return TWMC_OK;
 }
 
@@ -579,6 +595,8 @@ int download_real(twmc_handle* h, const DevBuf& b, double* out, size_t n) {
 // bounded per-handle buffer), each chunk copied straight to its rows by one
 // strided copy.
 constexpr size_t kWideChunk = size_t(1) << 25;  // 256 MB of doubles
+constexpr int kFinalChunks = 4;                  // trajectory ranges of the final-field pipeline
+constexpr size_t kSnapMax = size_t(8) << 30;     // largest final field (bytes) the pipeline stages
 
 int download_rows(twmc_handle* h, double* out, size_t row_stride) {
   const size_t rows = size_t(h->ntraj), row = size_t(2 * h->nsites);  // doubles per trajectory
@@ -738,6 +756,9 @@ void twmc_destroy(twmc_handle* h) {
   if (!h) return;
   cudaSetDevice(h->device);
   if (h->stream) cudaStreamSynchronize(h->stream);
+  if (h->dl_stream) cudaStreamSynchronize(h->dl_stream);
+  for (cudaEvent_t e : h->dl_ev) cudaEventDestroy(e);
+  if (h->dl_stream) cudaStreamDestroy(h->dl_stream);
   for (auto& e : h->ev_pending) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
   for (auto& e : h->ev_free) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
   if (h->stream) cudaStreamDestroy(h->stream);
@@ -932,6 +953,42 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
         }
         return TWMC_OK;
       };
+      // final-field pipeline: the steps that end the run go in kFinalChunks
+      // trajectory ranges, each range widened into d_snap and copied to the
+      // caller's rows on dl_stream while the next range computes (FP32,
+      // Philox noise, consecutive output rows, at least 2^20 sites)
+      const bool pipe = out && out->final_field && contiguous && h->prec == 0 && !h->thermo &&
+                        h->noise_mode == TWMC_NOISE_PHILOX && int64_t(bn) >= kFinalChunks &&
+                        int64_t(bn) * N >= (int64_t(1) << 20) && size_t(bn) * size_t(N) * 16 <= kSnapMax;
+      bool final_sent = false;
+      auto step = [&](int64_t nsteps, bool nk, bool last) -> int {
+        if (!(pipe && last && nsteps > 0)) return advance(h, nsteps, nk);
+        if (!h->dl_stream) TWMC_CUDA(h, cudaStreamCreateWithFlags(&h->dl_stream, cudaStreamNonBlocking));
+        while (h->dl_ev.size() < size_t(kFinalChunks)) {
+          cudaEvent_t e;
+          TWMC_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+          h->dl_ev.push_back(e);
+        }
+        const size_t row = size_t(2 * N);  // doubles per trajectory
+        if (!h->d_snap.ensure(size_t(bn) * row * sizeof(double))) return fail(h, TWMC_ERR_NOMEM, "final field buffer");
+        double* snap = h->d_snap.as<double>();
+        const float* st = static_cast<const float*>(h->d_state.p);
+        for (int c = 0; c < kFinalChunks; ++c) {
+          const int64_t t0 = int64_t(bn) * c / kFinalChunks, t1 = int64_t(bn) * (c + 1) / kFinalChunks;
+          int r2 = advance(h, nsteps, nk, t0, t1, false);
+          if (r2) return r2;
+          std::string err;
+          if (!widen_launch(st + size_t(t0) * row, snap + size_t(t0) * row, int64_t(size_t(t1 - t0) * row), h->stream, &err))
+            return fail(h, TWMC_ERR_CUDA, err);
+          TWMC_CUDA(h, cudaEventRecord(h->dl_ev[size_t(c)], h->stream));
+          TWMC_CUDA(h, cudaStreamWaitEvent(h->dl_stream, h->dl_ev[size_t(c)], 0));
+          TWMC_CUDA(h, cudaMemcpyAsync(out->final_field + (idx[0] + size_t(t0)) * row, snap + size_t(t0) * row,
+                                       size_t(t1 - t0) * row * sizeof(double), cudaMemcpyDeviceToHost, h->dl_stream));
+        }
+        h->step_pos += uint32_t(nsteps);
+        final_sent = true;
+        return TWMC_OK;
+      };
       int64_t f = 0, cur = 0;
       const bool want_nk = out && out->moments;
       if (std::get<2>(g.first) && s.n_frames > 0) {
@@ -940,7 +997,7 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
         if (rc) return rc;
       }
       for (int64_t ss : s.save_steps) {
-        rc = advance(h, ss - cur, want_nk);
+        rc = step(ss - cur, want_nk, ss == s.steps);
         if (rc) return rc;
         done_steps += (ss - cur) * int64_t(bn);
         cur = ss;
@@ -949,11 +1006,11 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
         h->progress = total_steps ? double(done_steps) / double(total_steps) : 1.0;
       }
       if (s.steps > cur) {
-        rc = advance(h, s.steps - cur, false);
+        rc = step(s.steps - cur, false, true);
         if (rc) return rc;
         done_steps += (s.steps - cur) * int64_t(bn);
       }
-      if (out && out->final_field) {
+      if (out && out->final_field && !final_sent) {  // (a pipelined run has sent it already)
         if (contiguous) {
           rc = download_rows(h, out->final_field + idx[0] * N * 2, size_t(N * 2));
           if (rc) return rc;
@@ -968,6 +1025,7 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
       std::vector<int> st(bn);
       TWMC_CUDA(h, cudaMemcpyAsync(st.data(), h->d_status.p, bn * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
       TWMC_CUDA(h, cudaStreamSynchronize(h->stream));
+      if (final_sent) TWMC_CUDA(h, cudaStreamSynchronize(h->dl_stream));
       for (size_t i = 0; i < bn; ++i) {
         if (out && out->status) out->status[idx[i]] = st[i];
         if (out && out->t_final) out->t_final[idx[i]] = s.t_final;

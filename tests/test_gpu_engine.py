@@ -224,6 +224,36 @@ def test_run_interleaved_groups_and_pinned_buffers(built_lib):
     s.close()
 
 
+def test_run_final_field_pipeline(built_lib):
+    """Runs of at least 2^20 sites send the final field through the pipeline
+    (the last steps in four trajectory ranges, each range copied to the host
+    while the next computes): equal to the last saved frame, to the same
+    trajectories stepped through the batch API, and into pinned arrays; a
+    run shorter than half a frame saves no frame and pipelines its trailing
+    steps."""
+    import torch
+    s = twmc.System(nx=32, ny=32, J=1.0, gamma=1.0, dt=0.002, frame_steps=25,
+                    omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=0.2, F=1.5, beta_init_sigma=0.5)
+    n = 1030
+    tasks = s.make_tasks(n, t_end=0.1, seed0=11, store_initial=False)
+    a = s.run(tasks, frames=True, final=True, moments=True)
+    assert np.array_equal(a["final"], a["frames"][:, -1])
+    pinned = {"final": torch.empty((n, 1024), dtype=torch.complex128, pin_memory=True).numpy()}
+    b = s.run(tasks, frames=False, final=True, buffers=pinned)
+    assert np.array_equal(b["final"], a["final"])
+    for t_end in (0.1, 0.02):
+        t2 = s.make_tasks(n, t_end=t_end, seed0=11, store_initial=False)
+        c = s.run(t2, frames=False, final=True)
+        steps = int(round(c["t_final"][0] / 0.002))
+        assert steps == (50 if t_end == 0.1 else 10)
+        s.batch_init(t2)
+        s.advance(steps)
+        s.sync()
+        field, _ = s.download(field=True, moments=False)
+        assert np.array_equal(c["final"], field), t_end
+    s.close()
+
+
 def test_run_into_caller_buffers(built_lib):
     """run() writes into caller-provided result arrays (reused across calls,
     e.g. pinned memory) exactly what it returns in arrays of its own; the
