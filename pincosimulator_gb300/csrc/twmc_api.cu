@@ -100,6 +100,7 @@ struct twmc_handle {
   // host on dl_stream while the next range computes
   cudaStream_t dl_stream = nullptr;
   std::vector<cudaEvent_t> dl_ev;
+  cudaEvent_t snap_ready = nullptr, snap_free = nullptr;  // d_snap written (stream) / read (dl_stream)
   DevBuf d_snap;
   std::vector<double> ft_times;   // with sentinel
   std::vector<cd> ft_vals, ft_slopes;
@@ -598,24 +599,30 @@ constexpr size_t kWideChunk = size_t(1) << 25;  // 256 MB of doubles
 constexpr int kFinalChunks = 4;                  // trajectory ranges of the final-field pipeline
 constexpr size_t kSnapMax = size_t(8) << 30;     // largest final field (bytes) the pipeline stages
 
+// m device rows of `row` doubles (consecutive) to host rows `row_stride`
+// doubles apart: one flat copy, one strided copy, or one copy per row when
+// the pitch exceeds the device's limit.
+cudaError_t copy_rows_d2h(int device, double* dst, size_t row_stride, const void* src_rows, size_t row, size_t m,
+                          cudaStream_t s) {
+  if (row_stride == row) return cudaMemcpyAsync(dst, src_rows, m * row * sizeof(double), cudaMemcpyDeviceToHost, s);
+  int maxpitch = 0;
+  cudaDeviceGetAttribute(&maxpitch, cudaDevAttrMaxPitch, device);
+  if (row_stride * sizeof(double) <= size_t(maxpitch))
+    return cudaMemcpy2DAsync(dst, row_stride * sizeof(double), src_rows, row * sizeof(double), row * sizeof(double), m,
+                             cudaMemcpyDeviceToHost, s);
+  for (size_t r = 0; r < m; ++r) {
+    const cudaError_t e = cudaMemcpyAsync(dst + r * row_stride, static_cast<const double*>(src_rows) + r * row,
+                                          row * sizeof(double), cudaMemcpyDeviceToHost, s);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 int download_rows(twmc_handle* h, double* out, size_t row_stride) {
   const size_t rows = size_t(h->ntraj), row = size_t(2 * h->nsites);  // doubles per trajectory
   if (rows == 0) return TWMC_OK;
-  int maxpitch = 0;
-  cudaDeviceGetAttribute(&maxpitch, cudaDevAttrMaxPitch, h->device);
-  const bool strided = row_stride * sizeof(double) <= size_t(maxpitch);
   auto copy_rows = [&](double* dst, const void* src_rows, size_t m) -> cudaError_t {
-    if (row_stride == row)  // consecutive rows: one flat copy
-      return cudaMemcpyAsync(dst, src_rows, m * row * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
-    if (strided)
-      return cudaMemcpy2DAsync(dst, row_stride * sizeof(double), src_rows, row * sizeof(double), row * sizeof(double), m,
-                               cudaMemcpyDeviceToHost, h->stream);
-    for (size_t r = 0; r < m; ++r) {  // pitch above the device limit: one copy per trajectory
-      const cudaError_t e = cudaMemcpyAsync(dst + r * row_stride, static_cast<const double*>(src_rows) + r * row,
-                                            row * sizeof(double), cudaMemcpyDeviceToHost, h->stream);
-      if (e != cudaSuccess) return e;
-    }
-    return cudaSuccess;
+    return copy_rows_d2h(h->device, dst, row_stride, src_rows, row, m, h->stream);
   };
   if (h->prec) {
     TWMC_CUDA(h, copy_rows(out, h->d_state.p, rows));
@@ -758,6 +765,8 @@ void twmc_destroy(twmc_handle* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   if (h->dl_stream) cudaStreamSynchronize(h->dl_stream);
   for (cudaEvent_t e : h->dl_ev) cudaEventDestroy(e);
+  if (h->snap_ready) cudaEventDestroy(h->snap_ready);
+  if (h->snap_free) cudaEventDestroy(h->snap_free);
   if (h->dl_stream) cudaStreamDestroy(h->dl_stream);
   for (auto& e : h->ev_pending) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
   for (auto& e : h->ev_free) { cudaEventDestroy(e.first); cudaEventDestroy(e.second); }
@@ -911,6 +920,82 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
       // field are copied to their places by strided asynchronous copies
       bool contiguous = true;
       for (size_t i = 1; i < bn && contiguous; ++i) contiguous = idx[i] == idx[0] + i;
+      // Staging for host copies on the handle's second stream (dl_stream): the
+      // batch widened into d_snap (FP32 runs, consecutive output rows, at
+      // most kSnapMax bytes) is copied to the caller while the next steps
+      // compute. snap_free (recorded on dl_stream after each copy from
+      // d_snap) orders the next write of d_snap after it.
+      const bool stage = contiguous && h->prec == 0 && size_t(bn) * size_t(N) * 16 <= kSnapMax &&
+                         int64_t(bn) * N >= (int64_t(1) << 20);
+      bool dl_used = false;
+      const size_t row = size_t(2 * N);  // doubles per trajectory
+      auto stage_setup = [&]() -> int {
+        if (!h->dl_stream) TWMC_CUDA(h, cudaStreamCreateWithFlags(&h->dl_stream, cudaStreamNonBlocking));
+        while (h->dl_ev.size() < size_t(kFinalChunks)) {
+          cudaEvent_t e;
+          TWMC_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+          h->dl_ev.push_back(e);
+        }
+        if (!h->snap_ready) TWMC_CUDA(h, cudaEventCreateWithFlags(&h->snap_ready, cudaEventDisableTiming));
+        if (!h->snap_free) TWMC_CUDA(h, cudaEventCreateWithFlags(&h->snap_free, cudaEventDisableTiming));
+        if (!h->d_snap.ensure(size_t(bn) * row * sizeof(double))) return fail(h, TWMC_ERR_NOMEM, "staging buffer");
+        dl_used = true;
+        return TWMC_OK;
+      };
+      // final-field pipeline: the steps that end the run go in kFinalChunks
+      // trajectory ranges, each range widened into d_snap and copied to the
+      // caller's rows on dl_stream while the next range computes (also Philox
+      // noise and no work / area)
+      const bool pipe = stage && out && out->final_field && !h->thermo && h->noise_mode == TWMC_NOISE_PHILOX &&
+                        int64_t(bn) >= kFinalChunks;
+      bool final_sent = false, frame_sent = false;
+      // fdst: the last saved frame's rows when this step ends on it (sent
+      // range by range as well)
+      auto step = [&](int64_t nsteps, bool nk, bool last, double* fdst) -> int {
+        if (!(pipe && last && nsteps > 0)) return advance(h, nsteps, nk);
+        int r2 = stage_setup();
+        if (r2) return r2;
+        double* snap = h->d_snap.as<double>();
+        const float* st = static_cast<const float*>(h->d_state.p);
+        for (int c = 0; c < kFinalChunks; ++c) {
+          const int64_t t0 = int64_t(bn) * c / kFinalChunks, t1 = int64_t(bn) * (c + 1) / kFinalChunks;
+          r2 = advance(h, nsteps, nk, t0, t1, false);
+          if (r2) return r2;
+          if (c == 0) TWMC_CUDA(h, cudaStreamWaitEvent(h->stream, h->snap_free, 0));
+          std::string err;
+          if (!widen_launch(st + size_t(t0) * row, snap + size_t(t0) * row, int64_t(size_t(t1 - t0) * row), h->stream, &err))
+            return fail(h, TWMC_ERR_CUDA, err);
+          TWMC_CUDA(h, cudaEventRecord(h->dl_ev[size_t(c)], h->stream));
+          TWMC_CUDA(h, cudaStreamWaitEvent(h->dl_stream, h->dl_ev[size_t(c)], 0));
+          TWMC_CUDA(h, cudaMemcpyAsync(out->final_field + (idx[0] + size_t(t0)) * row, snap + size_t(t0) * row,
+                                       size_t(t1 - t0) * row * sizeof(double), cudaMemcpyDeviceToHost, h->dl_stream));
+          if (fdst)
+            TWMC_CUDA(h, copy_rows_d2h(h->device, fdst + size_t(t0) * size_t(max_frames) * row, size_t(max_frames) * row,
+                                       snap + size_t(t0) * row, row, size_t(t1 - t0), h->dl_stream));
+        }
+        frame_sent = fdst != nullptr;
+        TWMC_CUDA(h, cudaEventRecord(h->snap_free, h->dl_stream));
+        h->step_pos += uint32_t(nsteps);
+        final_sent = true;
+        return TWMC_OK;
+      };
+      // a saved frame through d_snap (the last frame of a pipelined run is
+      // already staged there)
+      auto stage_frame = [&](double* dst) -> int {
+        int r2 = stage_setup();
+        if (r2) return r2;
+        if (!final_sent) {
+          TWMC_CUDA(h, cudaStreamWaitEvent(h->stream, h->snap_free, 0));
+          std::string err;
+          if (!widen_launch(h->d_state.p, h->d_snap.as<double>(), int64_t(size_t(bn) * row), h->stream, &err))
+            return fail(h, TWMC_ERR_CUDA, err);
+          TWMC_CUDA(h, cudaEventRecord(h->snap_ready, h->stream));
+          TWMC_CUDA(h, cudaStreamWaitEvent(h->dl_stream, h->snap_ready, 0));
+        }
+        TWMC_CUDA(h, copy_rows_d2h(h->device, dst, size_t(max_frames) * row, h->d_snap.p, row, size_t(bn), h->dl_stream));
+        TWMC_CUDA(h, cudaEventRecord(h->snap_free, h->dl_stream));
+        return TWMC_OK;
+      };
       auto save_frame = [&](int64_t f) -> int {
         if (out && out->moments) {
           int r2 = reduce(h);
@@ -925,7 +1010,13 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
           }
         }
         if (out && out->frames) {
-          if (contiguous) {
+          if (stage) {
+            if (!frame_sent) {
+              int r2 = stage_frame(out->frames + (idx[0] * max_frames + f) * N * 2);
+              if (r2) return r2;
+            }
+            frame_sent = false;
+          } else if (contiguous) {
             int r2 = download_rows(h, out->frames + (idx[0] * max_frames + f) * N * 2, size_t(max_frames * N * 2));
             if (r2) return r2;
           } else {
@@ -953,42 +1044,6 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
         }
         return TWMC_OK;
       };
-      // final-field pipeline: the steps that end the run go in kFinalChunks
-      // trajectory ranges, each range widened into d_snap and copied to the
-      // caller's rows on dl_stream while the next range computes (FP32,
-      // Philox noise, consecutive output rows, at least 2^20 sites)
-      const bool pipe = out && out->final_field && contiguous && h->prec == 0 && !h->thermo &&
-                        h->noise_mode == TWMC_NOISE_PHILOX && int64_t(bn) >= kFinalChunks &&
-                        int64_t(bn) * N >= (int64_t(1) << 20) && size_t(bn) * size_t(N) * 16 <= kSnapMax;
-      bool final_sent = false;
-      auto step = [&](int64_t nsteps, bool nk, bool last) -> int {
-        if (!(pipe && last && nsteps > 0)) return advance(h, nsteps, nk);
-        if (!h->dl_stream) TWMC_CUDA(h, cudaStreamCreateWithFlags(&h->dl_stream, cudaStreamNonBlocking));
-        while (h->dl_ev.size() < size_t(kFinalChunks)) {
-          cudaEvent_t e;
-          TWMC_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
-          h->dl_ev.push_back(e);
-        }
-        const size_t row = size_t(2 * N);  // doubles per trajectory
-        if (!h->d_snap.ensure(size_t(bn) * row * sizeof(double))) return fail(h, TWMC_ERR_NOMEM, "final field buffer");
-        double* snap = h->d_snap.as<double>();
-        const float* st = static_cast<const float*>(h->d_state.p);
-        for (int c = 0; c < kFinalChunks; ++c) {
-          const int64_t t0 = int64_t(bn) * c / kFinalChunks, t1 = int64_t(bn) * (c + 1) / kFinalChunks;
-          int r2 = advance(h, nsteps, nk, t0, t1, false);
-          if (r2) return r2;
-          std::string err;
-          if (!widen_launch(st + size_t(t0) * row, snap + size_t(t0) * row, int64_t(size_t(t1 - t0) * row), h->stream, &err))
-            return fail(h, TWMC_ERR_CUDA, err);
-          TWMC_CUDA(h, cudaEventRecord(h->dl_ev[size_t(c)], h->stream));
-          TWMC_CUDA(h, cudaStreamWaitEvent(h->dl_stream, h->dl_ev[size_t(c)], 0));
-          TWMC_CUDA(h, cudaMemcpyAsync(out->final_field + (idx[0] + size_t(t0)) * row, snap + size_t(t0) * row,
-                                       size_t(t1 - t0) * row * sizeof(double), cudaMemcpyDeviceToHost, h->dl_stream));
-        }
-        h->step_pos += uint32_t(nsteps);
-        final_sent = true;
-        return TWMC_OK;
-      };
       int64_t f = 0, cur = 0;
       const bool want_nk = out && out->moments;
       if (std::get<2>(g.first) && s.n_frames > 0) {
@@ -997,7 +1052,9 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
         if (rc) return rc;
       }
       for (int64_t ss : s.save_steps) {
-        rc = step(ss - cur, want_nk, ss == s.steps);
+        const bool last = ss == s.steps;
+        double* fdst = last && stage && out && out->frames ? out->frames + (idx[0] * max_frames + f) * N * 2 : nullptr;
+        rc = step(ss - cur, want_nk, last, fdst);
         if (rc) return rc;
         done_steps += (ss - cur) * int64_t(bn);
         cur = ss;
@@ -1006,7 +1063,7 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
         h->progress = total_steps ? double(done_steps) / double(total_steps) : 1.0;
       }
       if (s.steps > cur) {
-        rc = step(s.steps - cur, false, true);
+        rc = step(s.steps - cur, false, true, nullptr);
         if (rc) return rc;
         done_steps += (s.steps - cur) * int64_t(bn);
       }
@@ -1025,7 +1082,7 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
       std::vector<int> st(bn);
       TWMC_CUDA(h, cudaMemcpyAsync(st.data(), h->d_status.p, bn * sizeof(int), cudaMemcpyDeviceToHost, h->stream));
       TWMC_CUDA(h, cudaStreamSynchronize(h->stream));
-      if (final_sent) TWMC_CUDA(h, cudaStreamSynchronize(h->dl_stream));
+      if (dl_used) TWMC_CUDA(h, cudaStreamSynchronize(h->dl_stream));
       for (size_t i = 0; i < bn; ++i) {
         if (out && out->status) out->status[idx[i]] = st[i];
         if (out && out->t_final) out->t_final[idx[i]] = s.t_final;

@@ -225,9 +225,10 @@ def test_run_interleaved_groups_and_pinned_buffers(built_lib):
 
 
 def test_run_final_field_pipeline(built_lib):
-    """Runs of at least 2^20 sites send the final field through the pipeline
-    (the last steps in four trajectory ranges, each range copied to the host
-    while the next computes): equal to the last saved frame, to the same
+    """Runs of at least 2^20 sites stage saved frames on a second stream and
+    send the final field through the pipeline (the last steps in four
+    trajectory ranges, each range copied to the host while the next
+    computes): equal to the last saved frame, to the same
     trajectories stepped through the batch API, and into pinned arrays; a
     run shorter than half a frame saves no frame and pipelines its trailing
     steps."""
@@ -238,9 +239,17 @@ def test_run_final_field_pipeline(built_lib):
     tasks = s.make_tasks(n, t_end=0.1, seed0=11, store_initial=False)
     a = s.run(tasks, frames=True, final=True, moments=True)
     assert np.array_equal(a["final"], a["frames"][:, -1])
-    pinned = {"final": torch.empty((n, 1024), dtype=torch.complex128, pin_memory=True).numpy()}
-    b = s.run(tasks, frames=False, final=True, buffers=pinned)
-    assert np.array_equal(b["final"], a["final"])
+    pinned = {"final": torch.empty((n, 1024), dtype=torch.complex128, pin_memory=True).numpy(),
+              "frames": torch.empty((n, 2, 1024), dtype=torch.complex128, pin_memory=True).numpy()}
+    b = s.run(tasks, frames=True, final=True, buffers=pinned)
+    assert np.array_equal(b["final"], a["final"]) and np.array_equal(b["frames"], a["frames"])
+    # saved frames (staged on the second stream) against the batch API
+    s.batch_init(tasks)
+    for f in range(2):
+        s.advance(25)
+        s.sync()
+        field, _ = s.download(field=True, moments=False)
+        assert np.array_equal(a["frames"][:, f], field), f
     for t_end in (0.1, 0.02):
         t2 = s.make_tasks(n, t_end=t_end, seed0=11, store_initial=False)
         c = s.run(t2, frames=False, final=True)
