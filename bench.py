@@ -186,22 +186,12 @@ def measure_other_paths(twmc, torch, sm_mhz=None):
     out["heterogeneous_batch"] = {"value": FRAME_STEPS * sites / (ms / 1e3), "unit": METRIC, "points": len(pts),
                                   "ms_per_frame": ms, "autotuned": True}
     hb.close()
-    nc = 256
-    n = 3 * nc
-    times = np.round(np.arange(0, 40 + 1e-9, 0.01), 10)
-    vals = np.zeros((len(times), n), dtype=complex)
-    vals[:, 1::3] = (2.5 * times / 40.0)[:, None]
-    sysd = twmc.System(lattice=twmc.LATTICE_LIEB, nx=1, ny=nc, pbc=True, J_AB=1.0, J_BC=1.0, gamma=1.0,
-                       detuning=0.0, dt=DT, frame_steps=250, omega=0.0,
-                       U=twmc.Noisy(0.27, twmc.DISORDER_UNIFORM, 0.06), F=0.0, F_t=(times, vals),
-                       beta_init_sigma=0.5)
-    tasks = sysd.make_tasks(8192, t_end=2.0, store_initial=False)
-    sysd.run(tasks, frames=False, final=False)
-    t0 = time.perf_counter()
-    sysd.run(tasks, frames=False, final=False)
-    el = time.perf_counter() - t0
-    out["lieb"] = {"value": n * 8192 * 1000 / el, "unit": METRIC, "kernel": sysd.kernel_name,
-                   "timing": "host wall clock around twmc_run (initial draws and frame bookkeeping included)"}
+    from pincosimulator_gb300 import workloads
+    sysd = workloads.lieb()
+    el, _ = workloads.time_run(sysd, 8192, 4)
+    out["lieb"] = {"value": sysd.n_sites * 8192 * 1000 / el, "unit": METRIC, "kernel": sysd.kernel_name,
+                   "timing": "host wall clock around one twmc_run call of 1000 steps (initial draws and frame "
+                             "bookkeeping included)"}
     sysd.close()
     return out
 

@@ -1,0 +1,97 @@
+"""Named workloads of the GPU TWMC engine and a command line that runs one.
+
+* ``square64``  -- 2-D 64x64 PBC, J=1, U=0.2, gamma=1, omega=-0.5 with
+  Gaussian disorder of amplitude 0.2, F=2, dt=0.002, frames of 250 steps
+  (the headline workload; ``--hop stencil`` for the real-space kernel).
+* ``square128`` -- the same parameters on a 128x128 lattice (the 2-CTA
+  cluster stencil kernel, power-of-two form).
+* ``lieb768``   -- the 1-D Lieb lattice of 256 cells (768 sites), PBC,
+  J_AB=J_BC=1, gamma=1, U=0.27 with uniform disorder of amplitude 0.06, and a
+  drive F(t) on the B sites ramping from 0 to 2.5 over t in [0, 40] in
+  records every 0.01, then held (the configuration of
+  ``TWMCLiebSolver``'s F(t) runs).
+
+``python -m pincosimulator_gb300.workloads lieb768 --ntraj 2048 --frames 1``
+runs ``twmc_run`` over the given number of frames (after one untimed call)
+and prints the kernel, the wall time and the site-updates per second as one
+JSON line; square workloads are stepped through the device-resident batch
+API and timed with CUDA events on the library's stream.
+"""
+import argparse
+import json
+import time
+
+import numpy as np
+
+from . import twmc
+
+DT = 0.002
+FRAME_STEPS = 250
+
+
+def square(nx, ny, hop=twmc.HOP_FFT, precision=twmc.PREC_F32, n_moment_blocks=32):
+    return twmc.System(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=DT, frame_steps=FRAME_STEPS,
+                       omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=0.2, F=2.0, beta_init=0.0,
+                       beta_init_sigma=0.5, precision=precision, hop=hop, n_moment_blocks=n_moment_blocks)
+
+
+def lieb(ncell=256):
+    n = 3 * ncell
+    times = np.round(np.arange(0, 40 + 1e-9, 0.01), 10)
+    vals = np.zeros((len(times), n), dtype=complex)
+    vals[:, 1::3] = (2.5 * times / 40.0)[:, None]
+    return twmc.System(lattice=twmc.LATTICE_LIEB, nx=1, ny=ncell, pbc=True, J_AB=1.0, J_BC=1.0, gamma=1.0,
+                       detuning=0.0, dt=DT, frame_steps=FRAME_STEPS, omega=0.0,
+                       U=twmc.Noisy(0.27, twmc.DISORDER_UNIFORM, 0.06), F=0.0, F_t=(times, vals),
+                       beta_init_sigma=0.5)
+
+
+def time_run(sysd, ntraj, frames):
+    """Wall time of one twmc_run call of `frames` frames (after an untimed call)."""
+    tasks = sysd.make_tasks(ntraj, t_end=frames * FRAME_STEPS * DT, store_initial=False)
+    sysd.run(tasks, frames=False, final=False)
+    t0 = time.perf_counter()
+    res = sysd.run(tasks, frames=False, final=False)
+    return time.perf_counter() - t0, bool(np.all(res["status"] == 0))
+
+
+def time_batch(sysd, ntraj, frames):
+    """CUDA-event time of `frames` frames stepped through the batch API (after one untimed frame)."""
+    import torch
+
+    sysd.batch_init(sysd.make_tasks(ntraj, t_end=100.0))
+    sysd.advance(FRAME_STEPS)
+    sysd.sync()
+    ext = torch.cuda.ExternalStream(sysd.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(ext)
+    for _ in range(frames):
+        sysd.advance(FRAME_STEPS)
+    e1.record(ext)
+    sysd.sync()
+    return e0.elapsed_time(e1) / 1e3
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("workload", choices=["square64", "square128", "lieb768"])
+    ap.add_argument("--ntraj", type=int, default=2048)
+    ap.add_argument("--frames", type=int, default=1)
+    ap.add_argument("--hop", choices=["fft", "stencil"], default="stencil")
+    args = ap.parse_args(argv)
+    if args.workload == "lieb768":
+        sysd = lieb()
+        el, finite = time_run(sysd, args.ntraj, args.frames)
+    else:
+        L = 64 if args.workload == "square64" else 128
+        sysd = square(L, L, hop=twmc.HOP_STENCIL if args.hop == "stencil" else twmc.HOP_FFT)
+        el, finite = time_batch(sysd, args.ntraj, args.frames), True
+    line = {"workload": args.workload, "ntraj": args.ntraj, "frames": args.frames, "kernel": sysd.kernel_name,
+            "seconds": el, "site_updates_per_s": sysd.n_sites * args.ntraj * args.frames * FRAME_STEPS / el,
+            "finite": finite}
+    sysd.close()
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()
