@@ -109,7 +109,7 @@ struct twmc_handle {
   int bx = 0, by = 0;
   std::string kname;
   // device tables
-  DevBuf d_tw, d_ktab, d_nbr_idx, d_nbr_w, d_ft_vals, d_ft_slopes, d_ft_id, d_ft_dt;
+  DevBuf d_tw, d_ktab, d_nbr_idx, d_nbr_w, d_ft_vals, d_ft_slopes, d_ft_id, d_ft_dt, d_ft_dt_f;
   DevBuf d_shared_par[3];  // shared per-site rsl / iU / iF when not per-trajectory
   // batch
   int64_t ntraj = 0;
@@ -436,6 +436,7 @@ int advance(twmc_handle* h, int64_t n, bool want_nk, int64_t t0 = 0, int64_t t1 
     a.ft_slopes = h->d_ft_slopes.p;
     a.ft_id = h->d_ft_id.as<int>();
     a.ft_dt = h->d_ft_dt.as<double>();
+    a.ft_dt_f = h->d_ft_dt_f.as<float>();
   }
   if (h->thermo) {
     a.work = at(h->d_work.p, row_r);
@@ -901,7 +902,9 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
           offs[size_t(k)] = seg.second;
           hint = seg.first;
         }
-        if (!upload_raw(&h->d_ft_id, ids.data(), ids.size()) || !upload_raw(&h->d_ft_dt, offs.data(), offs.size()))
+        std::vector<float> offs_f(offs.begin(), offs.end());
+        if (!upload_raw(&h->d_ft_id, ids.data(), ids.size()) || !upload_raw(&h->d_ft_dt, offs.data(), offs.size()) ||
+            !upload_raw(&h->d_ft_dt_f, offs_f.data(), offs_f.size()))
           return fail(h, TWMC_ERR_NOMEM, "F(t) schedule upload");
       }
       // realisations of noisy matrices

@@ -65,6 +65,7 @@ struct StepArgs {
   const void* ft_slopes;  // [(nrec+1)][N] complex R: i dF/dt
   const int* ft_id;       // [total steps] segment id per step
   const double* ft_dt;    // [total steps] t - t_id per step
+  const float* ft_dt_f;   // the same in FP32 (no per-step conversion on the FP64 pipe)
   int dbuf;               // ell: double-buffered exchange
   // drive thermodynamics (ell kernel, TWMCThermoSolver.cpp:203-236): per-site
   // accumulators [ntraj][N] (R) of work 2 dt Re(beta) dF/dt and area
@@ -631,10 +632,12 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
       R dtt = R(0), dtp = R(0), seg_ratio = R(0);
       if (timedep) {
         id_t = a.ft_id[gstep];
-        dtt = R(a.ft_dt[gstep]);
-        id_p = gstep > 0 ? a.ft_id[gstep - 1] : id_t;
-        dtp = gstep > 0 ? R(a.ft_dt[gstep - 1]) : dtt;
-        if (!FAST && a.work != nullptr && gstep > 0) seg_ratio = R((a.ft_dt[gstep] - a.ft_dt[gstep - 1]) / a.dt);
+        dtt = F32 ? R(a.ft_dt_f[gstep]) : R(a.ft_dt[gstep]);
+        if (!FAST && a.work != nullptr) {  // work / area: the previous step's F(t)
+          id_p = gstep > 0 ? a.ft_id[gstep - 1] : id_t;
+          dtp = gstep > 0 ? (F32 ? R(a.ft_dt_f[gstep - 1]) : R(a.ft_dt[gstep - 1])) : dtt;
+          if (gstep > 0) seg_ratio = R((a.ft_dt[gstep] - a.ft_dt[gstep - 1]) / a.dt);
+        }
       }
       int rl = rl0, cl = cl0, rh = rh0, ch = ch0;
 #pragma unroll
