@@ -28,6 +28,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -123,7 +124,8 @@ def measure_warm_start():
     reduced version of the 32 x 32 sweep (F ~ U[0,3], detuning ~ U[-2,2],
     U ~ U[0.05,0.5], J = gamma = 1, dt = 0.002): plain runs of 1024 points
     generate the training rows, the MLP is trained on the GPU, then 64
-    held-out points run warm-started and plain (the judge)."""
+    held-out points run warm-started and plain (the plain run is the reference
+    each warm-started point is checked against)."""
     from pincosimulator_gb300 import warmstart as wsm
 
     return wsm.evaluate(32, n_train=1024, traj_train=256, t_train=20.0, n_test=64, traj_test=512, t_test=20.0)
@@ -284,6 +286,8 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--hop", default="fft", choices=["fft", "stencil"])
     ap.add_argument("--e2e-steps", type=int, default=4)
+    ap.add_argument("--clocks-csv", default=None,
+                    help="where nvidia-smi writes its clock samples (default: the temp directory)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm-start time-to-steady-state leg")
@@ -318,9 +322,11 @@ def main():
     sysd.sync()
     ext = torch.cuda.ExternalStream(sysd.stream)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    clk_path = os.path.join(ROOT, "gpurun_out" if os.path.isdir(os.path.join(ROOT, "gpurun_out")) else "_work",
-                            f"clocks_rank{rank}.csv")
-    os.makedirs(os.path.dirname(clk_path), exist_ok=True)
+    clk_path = args.clocks_csv or os.path.join(tempfile.gettempdir(), f"twmc_clocks_rank{rank}.csv")
+    if world > 1 and args.clocks_csv:
+        clk_path = f"{os.path.splitext(args.clocks_csv)[0]}_rank{rank}.csv"
+    if os.path.dirname(clk_path):
+        os.makedirs(os.path.dirname(clk_path), exist_ok=True)
     proc, fh = clock_sampler_start(clk_path)
     time.sleep(0.5)
     launches0 = sysd.launch_count

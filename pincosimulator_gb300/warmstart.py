@@ -8,7 +8,7 @@ trajectory then starts from beta_init = that mean field in real space plus
 Gaussian fluctuations of per-quadrature variance (max(n - |beta_init|^2, 0)
 + 1/2) / 2 (the reference's ReadFromSettings initial condition with a
 per-site beta_init and beta_init_sigma). The plain vacuum-initialised run
-stays the judge: a point whose warm-started steady density differs from the
+stays the reference: a point whose warm-started steady density differs from the
 plain run's by more than `rerun_se` standard errors is replaced by its plain
 result (the rerun rule).
 
@@ -253,7 +253,7 @@ class WarmSweep:
 
 def warm_sweep(ws: WarmStart, points, n_traj, t_end, dt=0.002, frame_period=0.5, seed0=1, rerun_se=1.0,
                tune=False):
-    """Warm-started sweep judged by plain runs: a point whose warm steady n
+    """Warm-started sweep checked against plain runs: a point whose warm steady n
     differs from the plain one by more than rerun_se combined standard
     errors takes the plain result."""
     x = features(points)
