@@ -931,6 +931,15 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
       const bool stage = contiguous && h->prec == 0 && size_t(bn) * size_t(N) * 16 <= kSnapMax &&
                          int64_t(bn) * N >= (int64_t(1) << 20);
       bool dl_used = false;
+      // copies into the caller's arrays may still be in flight when a group
+      // ends early with an error: drain both streams on every exit
+      struct Drain {
+        twmc_handle* h;
+        ~Drain() {
+          if (h->stream) cudaStreamSynchronize(h->stream);
+          if (h->dl_stream) cudaStreamSynchronize(h->dl_stream);
+        }
+      } drain{h};
       const size_t row = size_t(2 * N);  // doubles per trajectory
       auto stage_setup = [&]() -> int {
         if (!h->dl_stream) TWMC_CUDA(h, cudaStreamCreateWithFlags(&h->dl_stream, cudaStreamNonBlocking));
