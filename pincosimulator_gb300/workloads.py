@@ -5,6 +5,10 @@
   (the headline workload; ``--hop stencil`` for the real-space kernel).
 * ``square128`` -- the same parameters on a 128x128 lattice (the 2-CTA
   cluster stencil kernel, power-of-two form).
+* ``chain64``   -- the 1-D chain of 64 sites, J=1, U=0.1, gamma=1, omega=-1,
+  F=1.5, beta_init_sigma=0.5, dt=0.005, a frame every 100 steps: the
+  configuration of the reference's own CPU runs (1000 trajectories to
+  t = 50 there). Timed through ``twmc_run`` with every frame saved.
 * ``lieb768``   -- the 1-D Lieb lattice of 256 cells (768 sites), PBC,
   J_AB=J_BC=1, gamma=1, U=0.27 with uniform disorder of amplitude 0.06, and a
   drive F(t) on the B sites ramping from 0 to 2.5 over t in [0, 40] in
@@ -46,12 +50,18 @@ def lieb(ncell=256):
                        beta_init_sigma=0.5)
 
 
-def time_run(sysd, ntraj, frames):
-    """Wall time of one twmc_run call of `frames` frames (after an untimed call)."""
-    tasks = sysd.make_tasks(ntraj, t_end=frames * FRAME_STEPS * DT, store_initial=False)
-    sysd.run(tasks, frames=False, final=False)
+def chain64(hop=twmc.HOP_FFT):
+    return twmc.System(nx=1, ny=64, J=1.0, gamma=1.0, dt=0.005, frame_steps=100, omega=-1.0, U=0.1, F=1.5,
+                       beta_init=0.0, beta_init_sigma=0.5, hop=hop)
+
+
+def time_run(sysd, ntraj, frames, save=False):
+    """Wall time of one twmc_run call of `frames` frames (after an untimed
+    call); with `save`, every frame and the final field are returned."""
+    tasks = sysd.make_tasks(ntraj, t_end=frames * sysd.desc.frame_steps * sysd.desc.dt, store_initial=save)
+    sysd.run(tasks, frames=save, final=save)
     t0 = time.perf_counter()
-    res = sysd.run(tasks, frames=False, final=False)
+    res = sysd.run(tasks, frames=save, final=save)
     return time.perf_counter() - t0, bool(np.all(res["status"] == 0))
 
 
@@ -74,7 +84,7 @@ def time_batch(sysd, ntraj, frames):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("workload", choices=["square64", "square128", "lieb768"])
+    ap.add_argument("workload", choices=["square64", "square128", "lieb768", "chain64"])
     ap.add_argument("--ntraj", type=int, default=2048)
     ap.add_argument("--frames", type=int, default=1)
     ap.add_argument("--hop", choices=["fft", "stencil"], default="stencil")
@@ -82,12 +92,15 @@ def main(argv=None):
     if args.workload == "lieb768":
         sysd = lieb()
         el, finite = time_run(sysd, args.ntraj, args.frames)
+    elif args.workload == "chain64":
+        sysd = chain64(hop=twmc.HOP_STENCIL if args.hop == "stencil" else twmc.HOP_FFT)
+        el, finite = time_run(sysd, args.ntraj, args.frames, save=True)
     else:
         L = 64 if args.workload == "square64" else 128
         sysd = square(L, L, hop=twmc.HOP_STENCIL if args.hop == "stencil" else twmc.HOP_FFT)
         el, finite = time_batch(sysd, args.ntraj, args.frames), True
     line = {"workload": args.workload, "ntraj": args.ntraj, "frames": args.frames, "kernel": sysd.kernel_name,
-            "seconds": el, "site_updates_per_s": sysd.n_sites * args.ntraj * args.frames * FRAME_STEPS / el,
+            "seconds": el, "site_updates_per_s": sysd.n_sites * args.ntraj * args.frames * sysd.desc.frame_steps / el,
             "finite": finite}
     sysd.close()
     print(json.dumps(line), flush=True)
