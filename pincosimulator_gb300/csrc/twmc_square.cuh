@@ -26,7 +26,7 @@ constexpr int cta_for() {
 template <typename R, class P, bool FAST>
 bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo* info, std::string* err) {
   constexpr int CTA = cta_for<R, P>();
-  using Cfg = SquareCfg<P, CTA, R>;
+  using Cfg = SquareCfg<P, CTA, R, true>;  // as square_fft_kernel instantiates it
   (void)nparams;
   const StepArgs a2 = a;
   const size_t smem = Cfg::smem_bytes();
