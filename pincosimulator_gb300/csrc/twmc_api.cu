@@ -434,6 +434,11 @@ int advance(twmc_handle* h, int64_t n, bool want_nk, int64_t t0 = 0, int64_t t1 
   a.nbr_w = h->d_nbr_w.p;
   a.J = h->J;
   a.f_J = float(h->J);
+  a.lieb_pbc = h->pbc;
+  a.lieb_jab = h->J_AB;
+  a.lieb_jbc = h->J_BC;
+  a.f_lieb_jab = float(h->J_AB);
+  a.f_lieb_jbc = float(h->J_BC);
   if (h->timedep) {
     a.ft_vals = h->d_ft_vals.p;
     a.ft_slopes = h->d_ft_slopes.p;
@@ -458,7 +463,8 @@ int advance(twmc_handle* h, int64_t n, bool want_nk, int64_t t0 = 0, int64_t t1 
                       : square_launch_f64(h->bx, h->by, a, nparams, h->stream, &h->last_info, &err);
   } else {
     ok = ell_launch(h->prec, a, h->stream, &h->last_info, &err);
-    if (ok && std::strncmp(h->last_info.name, "ell_cluster", 11) == 0) h->kname = h->last_info.name;
+    if (ok && (std::strncmp(h->last_info.name, "ell_cluster", 11) == 0 || std::strcmp(h->last_info.name, "lieb_cell_kernel") == 0))
+      h->kname = h->last_info.name;
   }
   cudaEventRecord(ev.second, h->stream);
   h->ev_pending.push_back(ev);

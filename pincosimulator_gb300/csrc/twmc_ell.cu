@@ -42,6 +42,39 @@ int cluster_variant(const StepArgs& a) {
   return cluster_fast(a) ? kClusterPow2FastVariant : kClusterPow2Variant;
 }
 
+// Lieb lattice with whole cells per thread (lieb_cell_kernel): Nc even,
+// Nc / 2 threads per trajectory within one CTA, no work / area.
+constexpr int kLiebCta = 256;
+bool lieb_cell_ok(const StepArgs& a) {
+  const int64_t n = a.nsites;
+  return a.hop_kind == 0 && n % 6 == 0 && n / 6 >= 1 && n / 6 <= kLiebCta && a.work == nullptr;
+}
+
+template <typename R>
+bool lieb_cell_launch(const StepArgs& a0, cudaStream_t s, LaunchInfo* info, std::string* err) {
+  StepArgs a = a0;
+  const int tpt = int(a.nsites / 6), tpc = kLiebCta / tpt;
+  a.tpt = tpt;
+  a.dbuf = 1;
+  auto fn = lieb_cell_kernel<R, kLiebCta>;
+  const size_t smem = size_t(2) * tpc * size_t(a.nsites) * sizeof(c2_t<R>);
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) { cudaGetLastError(); if (err) *err = std::string("lieb smem: ") + cudaGetErrorString(e); return false; }
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, kLiebCta, smem);
+  if (e != cudaSuccess || per_sm <= 0) { cudaGetLastError(); if (err) *err = "lieb kernel does not fit on an SM"; return false; }
+  const int64_t groups = (a.ntraj + tpc - 1) / tpc;
+  const int grid = int(std::min<int64_t>(groups, int64_t(sms) * per_sm));
+  if (info) { info->name = "lieb_cell_kernel"; info->cta = kLiebCta; info->grid = grid; info->smem = smem; info->blocks_per_sm = per_sm; }
+  if (grid <= 0) return true;
+  fn<<<grid, kLiebCta, smem, s>>>(a);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) { if (err) *err = std::string("lieb launch: ") + cudaGetErrorString(e); return false; }
+  return true;
+}
+
 bool cluster_config(const void* fn, int64_t ntraj, int64_t nsites, size_t static_smem, int* grid, size_t* smem_out,
                     std::string* err) {
   const int64_t half = (nsites + 1) / 2, q = (half + 1) / 2;
@@ -138,6 +171,7 @@ bool ell_launch_dev(int prec, int variant, int hop, const StepArgs* dev_args, in
 
 bool ell_launch(int prec, const StepArgs& a, cudaStream_t s, LaunchInfo* info, std::string* err) {
   if (use_cluster(prec, a)) return cluster_launch(a, s, info, err);
+  if (lieb_cell_ok(a)) return prec == 0 ? lieb_cell_launch<float>(a, s, info, err) : lieb_cell_launch<double>(a, s, info, err);
   if (use_fast(prec, a)) return ell_launch_fast_f32(a, s, info, err);
   if (a.hop_kind == 0)
     return prec == 0 ? ell_pick<float, 0, false>(a, s, info, err) : ell_pick<double, 0, false>(a, s, info, err);

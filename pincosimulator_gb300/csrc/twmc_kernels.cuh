@@ -60,6 +60,10 @@ struct StepArgs {
   const int* nbr_idx;     // [N][4]
   const void* nbr_w;      // [N][4] complex R (h = sum w beta_idx)
   double J;
+  // Lieb couplings for the cell kernel (TWMCLiebSolver.cpp:52-85)
+  int lieb_pbc;
+  double lieb_jab, lieb_jbc;
+  float f_lieb_jab, f_lieb_jbc;
   // F(t) (ell kernel)
   const void* ft_vals;    // [(nrec+1)][N] complex R: i F at the records
   const void* ft_slopes;  // [(nrec+1)][N] complex R: i dF/dt
@@ -727,6 +731,156 @@ __global__ void __launch_bounds__(CTA) ell_kernel_dev(const StepArgs* __restrict
     reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(ap)[i];
   __syncthreads();
   ell_body<R, VPT, CTA, HOP, FAST>(s_a, smem_raw);
+}
+
+// ------------------------------------------------------------------------
+// 1-D Lieb lattice with whole cells per thread: thread t of a trajectory
+// holds cells t and t + Nc/2 (sites 3c, 3c+1, 3c+2 = A, B, C of cell c), so
+// each Philox pair (p, p + N/2) is one thread's, the couplings inside a cell
+// (A-B, B-C) use registers, and only C of the previous cell and B of the next
+// cell come from the other threads' shared-memory slices. The neighbour
+// table of the general kernel pads every site to four entries (A has one
+// coupling, B three, C two); here each site sums its own couplings in the
+// table's order (ascending neighbour index), each product (-i J) b rounded
+// once, so the FP32 results equal the table kernel's. Couplings of
+// TWMCLiebSolver::Setup (TWMCLiebSolver.cpp:52-85): A(3i)-B(3i+1) J_AB,
+// B(3i+1)-C(3i+2) J_BC, C(3i+2)-B(3(i+1)+1) J_BC, with PBC
+// C(3(Nc-1)+2)-B(1). Nc even, Nc / 2 <= CTA; no work / area.
+// ------------------------------------------------------------------------
+template <typename R, int CTA>
+__device__ __forceinline__ void lieb_cell_body(const StepArgs& a, unsigned char* smem_raw) {
+  using T = c2_t<R>;
+  T* s_b = reinterpret_cast<T*>(smem_raw);
+  const int N = int(a.nsites), nc = N / 3, half = N / 2, tpt = nc / 2;
+  const int tpc = CTA / tpt;
+  const int tid = threadIdx.x, slot = tid / tpt, t = tid % tpt;
+  const bool in_slot = slot < tpc;
+  constexpr bool F32 = sizeof(R) == 4;
+  const R jab = F32 ? R(a.f_lieb_jab) : R(a.lieb_jab), jbc = F32 ? R(a.f_lieb_jbc) : R(a.lieb_jbc);
+  const R dt = F32 ? R(a.f_dt) : R(a.dt), dt4 = F32 ? R(a.f_dt4) : R(a.dt4);
+  const T rsl_s = F32 ? cmake<T>(R(a.f_par[0]), R(a.f_par[1])) : cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
+  const T iU_s = F32 ? cmake<T>(R(a.f_par[2]), R(a.f_par[3])) : cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
+  const T iF_s = F32 ? cmake<T>(R(a.f_par[4]), R(a.f_par[5])) : cmake<T>(R(a.iF_s[0]), R(a.iF_s[1]));
+  const bool pbc = a.lieb_pbc != 0;
+  const bool timedep = a.ft_vals != nullptr;
+  // (-i J) b, each component rounded once
+  auto hj = [](R j, T b) -> T { return cmake<T>(j * b.y, -(j * b.x)); };
+  const T zero = cmake<T>(R(0), R(0));
+  // neighbours outside the thread's cells, per held cell k: C of the previous
+  // cell and B of the next one (-1: none, open boundary)
+  int prev_c[2], next_b[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int c = t + k * tpt;
+    prev_c[k] = c > 0 ? 3 * c - 1 : (pbc ? N - 1 : -1);
+    next_b[k] = c < nc - 1 ? 3 * c + 4 : (pbc ? 1 : -1);
+  }
+  const int64_t ngroups = (a.ntraj + tpc - 1) / tpc;
+  int buf = 0;
+  for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const int64_t traj = g * tpc + slot;
+    const bool active = in_slot && traj < a.ntraj;
+    const int64_t tr = active ? traj : 0;
+    T* st = reinterpret_cast<T*>(a.state) + tr * N;
+    const T* __restrict__ g_rsl = a.rsl ? reinterpret_cast<const T*>(a.rsl) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iU = a.iU ? reinterpret_cast<const T*>(a.iU) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iF = a.iF ? reinterpret_cast<const T*>(a.iF) + tr * a.par_stride : nullptr;
+    T b[6];  // cell t: A, B, C; cell t + Nc/2: A, B, C
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      b[j] = active ? st[3 * t + j] : zero;
+      b[3 + j] = active ? st[half + 3 * t + j] : zero;
+    }
+    const uint32_t seed = a.seeds[tr], id = a.ids[tr];
+    const T* noise_tr = reinterpret_cast<const T*>(a.noise) + tr * a.noise_traj_stride;
+    for (int64_t step = 0; step < a.nsteps; ++step) {
+      const uint32_t gstep = a.step0 + uint32_t(step);
+      T* sb = s_b + (a.dbuf ? buf : 0) * int64_t(tpc) * N + int64_t(in_slot ? slot : 0) * N;
+      const uint32_t sba = smem_addr(sb);
+      if (in_slot) {
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          sts_c(sba + uint32_t(3 * t + j) * uint32_t(sizeof(T)), b[j]);
+          sts_c(sba + uint32_t(half + 3 * t + j) * uint32_t(sizeof(T)), b[3 + j]);
+        }
+      }
+      __syncthreads();
+      T h[6];
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const int c = t + k * tpt;
+        const T A = b[3 * k], B = b[3 * k + 1], C = b[3 * k + 2];
+        const T cp = prev_c[k] >= 0 ? lds_c(sba + uint32_t(prev_c[k]) * uint32_t(sizeof(T)), T{}) : zero;
+        const T bn = next_b[k] >= 0 ? lds_c(sba + uint32_t(next_b[k]) * uint32_t(sizeof(T)), T{}) : zero;
+        h[3 * k] = hj(jab, B);
+        // B: neighbours in ascending index -- C of the previous cell first,
+        // except in cell 0, where it wraps to the last site
+        if (c > 0) {
+          h[3 * k + 1] = cadd(cadd(hj(jbc, cp), hj(jab, A)), hj(jbc, C));
+        } else {
+          const T s = cadd(hj(jab, A), hj(jbc, C));
+          h[3 * k + 1] = prev_c[k] >= 0 ? cadd(s, hj(jbc, cp)) : s;
+        }
+        // C: B of its cell, then B of the next cell -- first in the last cell,
+        // where the next B wraps to site 1
+        if (c < nc - 1) {
+          h[3 * k + 2] = cadd(hj(jbc, B), hj(jbc, bn));
+        } else {
+          h[3 * k + 2] = next_b[k] >= 0 ? cadd(hj(jbc, bn), hj(jbc, B)) : hj(jbc, B);
+        }
+      }
+      int id_t = 0;
+      R dtt = R(0);
+      if (timedep) {
+        id_t = a.ft_id[gstep];
+        dtt = F32 ? R(a.ft_dt_f[gstep]) : R(a.ft_dt[gstep]);
+      }
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        T xi_lo, xi_hi;
+        const int plo = 3 * t + j, phi = half + plo;
+        if (a.noise_mode == 0) {
+          const u32x4 w = wiener_words(uint32_t(plo), gstep, seed, id);
+          xi_lo = normal_pair(w.x, w.y, R(0));
+          xi_hi = normal_pair(w.z, w.w, R(0));
+        } else {
+          const T* nz = noise_tr + int64_t(gstep) * N;
+          xi_lo = nz[plo];
+          xi_hi = nz[phi];
+        }
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+          const int p = q ? phi : plo, v = q ? 3 + j : j;
+          const T r = g_rsl ? __ldg(g_rsl + p) : rsl_s;
+          const T u = g_iU ? __ldg(g_iU + p) : iU_s;
+          T f = g_iF ? __ldg(g_iF + p) : iF_s;
+          if (timedep) {
+            const T f0 = __ldg(reinterpret_cast<const T*>(a.ft_vals) + int64_t(id_t) * N + p);
+            const T f1 = __ldg(reinterpret_cast<const T*>(a.ft_slopes) + int64_t(id_t) * N + p);
+            f = cmake<T>(f0.x + dtt * f1.x, f0.y + dtt * f1.y);
+          }
+          b[v] = local_update(b[v], h[v], r, u, f, dt, dt4, q ? xi_hi : xi_lo);
+        }
+      }
+      if (a.dbuf) buf ^= 1; else __syncthreads();
+    }
+    if (active) {
+      bool bad = false;
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        st[3 * t + j] = b[j];
+        st[half + 3 * t + j] = b[3 + j];
+        bad |= !finite_c(b[j]) || !finite_c(b[3 + j]);
+      }
+      set_status(a.status, traj, bad);
+    }
+  }
+}
+
+template <typename R, int CTA>
+__global__ void __launch_bounds__(CTA) lieb_cell_kernel(const StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  lieb_cell_body<R, CTA>(a, smem_raw);
 }
 
 // ------------------------------------------------------------------------

@@ -109,13 +109,18 @@ def test_per_site_parameters(built_lib, oracle):
 
 
 @pytest.mark.parametrize("prec", [twmc.PREC_F32, twmc.PREC_F64])
-@pytest.mark.parametrize("ncell,pbc", [(256, True), (24, False), (1, True), (7, True)])
-def test_lieb_parity(built_lib, oracle, ncell, pbc, prec):
+@pytest.mark.parametrize("ncell,pbc,jab,jbc", [(256, True, 1.0, 1.0), (24, False, 1.0, 1.0), (1, True, 1.0, 1.0),
+                                               (7, True, 1.0, 1.0), (2, True, 1.3, 0.7), (2, False, 1.3, 0.7),
+                                               (30, True, 0.6, 1.4)])
+def test_lieb_parity(built_lib, oracle, ncell, pbc, jab, jbc, prec):
+    """An even number of cells runs the cell kernel (whole cells per thread),
+    an odd number the neighbour-table kernel; J_AB != J_BC checks that each
+    coupling lands on its bond."""
     rng = np.random.default_rng(ncell)
     E = 0.1 * rng.normal(size=3 * ncell)
     U = 0.27 + 0.06 * rng.random(size=3 * ncell)
-    res, refs = lieb_case(oracle, ncell, pbc=pbc, prec=prec, E=E, U=U, F=0.3, detuning=0.5)
-    assert res["kernel"] == "ell_kernel<table>"
+    res, refs = lieb_case(oracle, ncell, pbc=pbc, prec=prec, E=E, U=U, F=0.3, detuning=0.5, J_AB=jab, J_BC=jbc)
+    assert res["kernel"] == ("lieb_cell_kernel" if ncell % 2 == 0 else "ell_kernel<table>")
     check(res, refs, prec)
 
 
