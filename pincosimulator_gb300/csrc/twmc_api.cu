@@ -463,7 +463,8 @@ int advance(twmc_handle* h, int64_t n, bool want_nk, int64_t t0 = 0, int64_t t1 
                       : square_launch_f64(h->bx, h->by, a, nparams, h->stream, &h->last_info, &err);
   } else {
     ok = ell_launch(h->prec, a, h->stream, &h->last_info, &err);
-    if (ok && (std::strncmp(h->last_info.name, "ell_cluster", 11) == 0 || std::strcmp(h->last_info.name, "lieb_cell_kernel") == 0))
+    if (ok && (std::strncmp(h->last_info.name, "ell_cluster", 11) == 0 || std::strcmp(h->last_info.name, "lieb_cell_kernel") == 0 ||
+               std::strcmp(h->last_info.name, "rowrun_kernel") == 0))
       h->kname = h->last_info.name;
   }
   cudaEventRecord(ev.second, h->stream);

@@ -46,6 +46,20 @@ __device__ __forceinline__ double2 lds_c(uint32_t a, double2) {
   asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(a) : "memory");
   return v;
 }
+// Four consecutive FP32 complex values (32 bytes, 16-byte aligned) to / from
+// shared memory.
+__device__ __forceinline__ void lds_run4(uint32_t a, float2* v) {
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v[0].x), "=f"(v[0].y), "=f"(v[1].x), "=f"(v[1].y) : "r"(a) : "memory");
+  asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];"
+               : "=f"(v[2].x), "=f"(v[2].y), "=f"(v[3].x), "=f"(v[3].y) : "r"(a + 16u) : "memory");
+}
+__device__ __forceinline__ void sts_run4(uint32_t a, const float2* v) {
+  asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a), "f"(v[0].x), "f"(v[0].y), "f"(v[1].x), "f"(v[1].y)
+               : "memory");
+  asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a + 16u), "f"(v[2].x), "f"(v[2].y), "f"(v[3].x),
+               "f"(v[3].y) : "memory");
+}
 // Four consecutive reals from shared memory (16-byte aligned for FP32).
 __device__ __forceinline__ void lds_r4(uint32_t a, float* w) {
   asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(w[0]), "=f"(w[1]), "=f"(w[2]), "=f"(w[3]) : "r"(a) : "memory");

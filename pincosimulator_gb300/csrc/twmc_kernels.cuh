@@ -734,6 +734,129 @@ __global__ void __launch_bounds__(CTA) ell_kernel_dev(const StepArgs* __restrict
 }
 
 // ------------------------------------------------------------------------
+// Square stencil with runs of four sites along a row per thread (FP32, the
+// fast run: Philox noise, no F(t), no work / area). Thread t of a trajectory
+// holds sites 4t..4t+3 and their Philox partners N/2 + 4t..N/2 + 4t + 3
+// (ny and N/2 multiples of 4, so a run never crosses a row end). The runs
+// go to shared memory in two 16-byte stores; per run the rows above and
+// below arrive in two 16-byte loads each and the left / right ends in one
+// load each, while the neighbours inside the run are the thread's own
+// registers -- 1.5 loads per site-update instead of 4. The sums keep the
+// order of ell_body's stencil (right + left, then down + up), so results
+// equal the real-space kernel's.
+// ------------------------------------------------------------------------
+template <int CTA>
+__device__ __forceinline__ void rowrun_body(const StepArgs& a, unsigned char* smem_raw) {
+  using T = float2;
+  T* s_b = reinterpret_cast<T*>(smem_raw);
+  const int N = int(a.nsites), half = N / 2, nx = int(a.nx), ny = int(a.ny);
+  const int tpt = half / 4, tpc = CTA / tpt;
+  const int tid = threadIdx.x, slot = tid / tpt, t = tid % tpt;
+  const bool in_slot = slot < tpc;
+  const float J = a.f_J, dt = a.f_dt, dt4 = a.f_dt4;
+  const T rsl_s = make_float2(a.f_par[0], a.f_par[1]);
+  const T iU_s = make_float2(a.f_par[2], a.f_par[3]);
+  const T iF_s = make_float2(a.f_par[4], a.f_par[5]);
+  const float wy = ny > 1 ? 1.f : 0.f, wx = nx > 1 ? 1.f : 0.f;
+  constexpr uint32_t TS = uint32_t(sizeof(T));
+  // per run k: first site, and the sites of its up / down rows and of its
+  // left / right ends (periodic)
+  int p0[2], up[2], dn[2], lf[2], rt[2];
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int p = k * half + 4 * t, r = p / ny, c = p % ny;
+    p0[k] = p;
+    up[k] = (r > 0 ? r - 1 : nx - 1) * ny + c;
+    dn[k] = (r + 1 < nx ? r + 1 : 0) * ny + c;
+    lf[k] = r * ny + (c > 0 ? c - 1 : ny - 1);
+    rt[k] = r * ny + (c + 4 < ny ? c + 4 : 0);
+  }
+  const int64_t ngroups = (a.ntraj + tpc - 1) / tpc;
+  int buf = 0;
+  for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+    const int64_t traj = g * tpc + slot;
+    const bool active = in_slot && traj < a.ntraj;
+    const int64_t tr = active ? traj : 0;
+    T* st = reinterpret_cast<T*>(a.state) + tr * N;
+    const T* __restrict__ g_rsl = a.rsl ? reinterpret_cast<const T*>(a.rsl) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iU = a.iU ? reinterpret_cast<const T*>(a.iU) + tr * a.par_stride : nullptr;
+    const T* __restrict__ g_iF = a.iF ? reinterpret_cast<const T*>(a.iF) + tr * a.par_stride : nullptr;
+    T v[2][4];
+#pragma unroll
+    for (int k = 0; k < 2; ++k)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) v[k][j] = active ? st[p0[k] + j] : make_float2(0.f, 0.f);
+    const uint32_t seed = a.seeds[tr], id = a.ids[tr];
+    for (int64_t step = 0; step < a.nsteps; ++step) {
+      const uint32_t gstep = a.step0 + uint32_t(step);
+      T* sb = s_b + (a.dbuf ? buf : 0) * int64_t(tpc) * N + int64_t(in_slot ? slot : 0) * N;
+      const uint32_t sba = smem_addr(sb);
+      if (in_slot) {
+        sts_run4(sba + uint32_t(p0[0]) * TS, v[0]);
+        sts_run4(sba + uint32_t(p0[1]) * TS, v[1]);
+      }
+      __syncthreads();
+      T h[2][4];
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        T U[4], D[4];
+        lds_run4(sba + uint32_t(up[k]) * TS, U);
+        lds_run4(sba + uint32_t(dn[k]) * TS, D);
+        const T L = lds_c(sba + uint32_t(lf[k]) * TS, T{}), Rr = lds_c(sba + uint32_t(rt[k]) * TS, T{});
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          const T right = j < 3 ? v[k][j + 1] : Rr, left = j > 0 ? v[k][j - 1] : L;
+          const T sy = cadd(right, left), sx = cadd(D[j], U[j]);
+          const T s = make_float2(wy * sy.x + wx * sx.x, wy * sy.y + wx * sx.y);
+          h[k][j] = make_float2(J * s.y, -J * s.x);  // -i J s
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const u32x4 w = wiener_words(uint32_t(p0[0] + j), gstep, seed, id);
+        const T xi[2] = {normal_pair(w.x, w.y, 0.0f), normal_pair(w.z, w.w, 0.0f)};
+#pragma unroll
+        for (int k = 0; k < 2; ++k) {
+          const int p = p0[k] + j;
+          const T r = g_rsl ? __ldg(g_rsl + p) : rsl_s;
+          const T u = g_iU ? __ldg(g_iU + p) : iU_s;
+          const T f = g_iF ? __ldg(g_iF + p) : iF_s;
+          v[k][j] = local_update(v[k][j], h[k][j], r, u, f, dt, dt4, xi[k]);
+        }
+      }
+      if (a.dbuf) buf ^= 1; else __syncthreads();
+    }
+    if (active) {
+      bool bad = false;
+#pragma unroll
+      for (int k = 0; k < 2; ++k)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          st[p0[k] + j] = v[k][j];
+          bad |= !finite_c(v[k][j]);
+        }
+      set_status(a.status, traj, bad);
+    }
+  }
+}
+
+template <int CTA>
+__global__ void __launch_bounds__(CTA, 1) rowrun_kernel(const StepArgs a) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  rowrun_body<CTA>(a, smem_raw);
+}
+
+template <int CTA>
+__global__ void __launch_bounds__(CTA, 1) rowrun_kernel_dev(const StepArgs* __restrict__ ap) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) StepArgs s_a;
+  for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += CTA)
+    reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(ap)[i];
+  __syncthreads();
+  rowrun_body<CTA>(s_a, smem_raw);
+}
+
+// ------------------------------------------------------------------------
 // 1-D Lieb lattice with whole cells per thread: thread t of a trajectory
 // holds cells t and t + Nc/2 (sites 3c, 3c+1, 3c+2 = A, B, C of cell c), so
 // each Philox pair (p, p + N/2) is one thread's, the couplings inside a cell

@@ -80,6 +80,33 @@ def test_cluster_pow2_philox(built_lib, oracle, shape, site_omega):
         assert rel_err(res["final"][k], ref["final"]) < 1e-4
 
 
+@pytest.mark.parametrize("shape,site_omega", [((64, 64), True), ((64, 64), False), ((1, 4096), True),
+                                              ((16, 256), False), ((256, 16), True), ((1024, 4), False)])
+def test_rowrun_philox(built_lib, oracle, shape, site_omega):
+    """FP32 Philox runs of the real-space stencil on 4096 sites take the
+    row-run kernel (four sites along a row per thread; ny = 4 makes a run a
+    whole row) and agree with the oracle's Philox stream."""
+    nx, ny = shape
+    n = nx * ny
+    ntraj, steps, dt = 2, 60, 0.005
+    rng = np.random.default_rng(21)
+    beta0 = 0.3 * (rng.normal(size=(ntraj, n)) + 1j * rng.normal(size=(ntraj, n)))
+    omega = -0.5 + 0.2 * rng.normal(size=n) if site_omega else -0.5
+    sysd = twmc.System(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=dt, frame_steps=50, omega=omega, U=0.2, F=1.5,
+                       precision=twmc.PREC_F32, noise=twmc.NOISE_PHILOX, hop=twmc.HOP_STENCIL)
+    seeds = [5, 77]
+    tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=steps * dt, ic=twmc.IC_GIVEN, init_field=beta0, seeds=seeds,
+                            id0=3)
+    res = sysd.run(tasks, frames=False)
+    kernel = sysd.kernel_name
+    sysd.close()
+    assert kernel == "rowrun_kernel"
+    for k in range(ntraj):
+        ref = oracle.base_run(nx, ny, 1.0, 1.0, dt, 0.0, steps * dt, 50, 2, True, omega, 0.2, 1.5, beta0[k],
+                              seed=seeds[k], tid=3 + k, noise="philox32")
+        assert rel_err(res["final"][k], ref["final"]) < 1e-4
+
+
 def test_cluster_per_site_parameters(built_lib, oracle):
     rng = np.random.default_rng(6)
     n = 128 * 128
