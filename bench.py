@@ -162,13 +162,15 @@ def measure_other_paths(twmc, torch, sm_mhz=None):
     ms = e0.elapsed_time(e1) / 2
     out["headline_real_space"] = {"value": FRAME_STEPS * NTRAJ * NX * NY / (ms / 1e3), "unit": METRIC,
                                   "kernel": sysd.kernel_name, "ms_per_frame": ms}
-    ipsu = _profile_figure("inst_per_site_update", "ell_kernel_64x64_stencil.md")
+    kname = out["headline_real_space"]["kernel"]
+    prof = "rowrun_kernel_64x64.md" if kname == "rowrun_kernel" else "ell_kernel_64x64_stencil.md"
+    ipsu = _profile_figure("inst_per_site_update", prof)
     if ipsu and sm_mhz:
         sms = torch.cuda.get_device_properties(0).multi_processor_count
         ach = out["headline_real_space"]["value"] * ipsu / 32.0
         out["headline_real_space"]["issue"] = {
             "inst_per_site_update": ipsu, "frac": ach / (sms * 4 * sm_mhz * 1e6),
-            "source": "ncu instruction count (profiles/ell_kernel_64x64_stencil.md) x measured rate; "
+            "source": f"ncu instruction count (profiles/{prof}) x measured rate; "
                       "peak = SMs x 4 schedulers x median SM clock of the headline run"}
     sysd.close()
     rng = np.random.default_rng(3)
