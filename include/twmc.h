@@ -197,7 +197,13 @@ TWMC_API int twmc_batch_download(twmc_handle* h, double* field, double* moments)
 /* Kernel launches issued by this handle since creation (trajectory steps,
  * reductions, initialisation). */
 TWMC_API int64_t twmc_launch_count(const twmc_handle* h);
-/* Name of the step kernel variant the handle selected. */
+/* Name of the step kernel variant the handle selected: "square_fft_kernel"
+ * (register FFT), "ell_kernel<stencil>" / "ell_kernel<table>" (real space,
+ * square stencil / Lieb neighbour table), "rowrun_kernel" (square stencil,
+ * 4096 sites, FP32 Philox runs), "lieb_cell_kernel" (Lieb lattice, even
+ * number of cells), "ell_cluster_pow2_kernel" / "ell_cluster_kernel" (square
+ * stencil above 8192 sites on 2-CTA clusters). Kernels chosen at launch time
+ * are reported after the first step. */
 TWMC_API const char* twmc_kernel_name(const twmc_handle* h);
 /* The CUDA stream (cudaStream_t) all of the handle's work is issued on, for
  * callers that order their own work or record events against it. */
