@@ -63,3 +63,35 @@ def test_site_pairing_matches_numpy(oracle):
         a32 = oracle.site_normals(11, 5, 3, 0, n, f32=True)
         b32 = npo.site_normals(11, 5, 3, 0, n, f32_flavour=True)
         assert np.allclose(a32, b32, rtol=0, atol=1e-6)
+
+
+def test_wiener_stream_key_layout(oracle):
+    """The Wiener stream (stream 0) uses the fixed key with the trajectory in
+    the counter, (site pair, step, id, seed); the other streams the key
+    (seed, id) with counter (site pair, 0, stream, 0)."""
+    seed, tid, step, n = 123456789, 42, 17, 10
+    z = oracle.site_normals(seed, tid, step, 0, n)
+    ctr = np.array([[p, step, tid, seed] for p in range(5)], dtype=np.uint32)
+    w = npo.philox4x32_10(ctr, np.broadcast_to(np.array(npo.WIENER_KEY, np.uint32), (5, 2)))
+    a, b = w[0, 0].astype(np.float64), w[0, 1].astype(np.float64)
+    u1, u2 = (a + 0.5) * 2.0 ** -32, (b + 0.5) * 2.0 ** -32
+    z0 = np.sqrt(-2 * np.log(u1)) * complex(np.cos(2 * np.pi * u2 - np.pi), np.sin(2 * np.pi * u2 - np.pi))
+    assert abs(z[0] - z0) < 1e-12
+    # an init-stream draw is keyed by (seed, id) instead
+    zi = oracle.site_normals(seed, tid, 0, 1, n)
+    w1 = npo.philox4x32_10(np.array([[0, 0, 1, 0]], np.uint32), np.array([[seed, tid]], np.uint32))
+    u1, u2 = (w1[0, 0] + 0.5) * 2.0 ** -32, (w1[0, 1] + 0.5) * 2.0 ** -32
+    assert abs(zi[0] - np.sqrt(-2 * np.log(u1)) * np.exp(1j * (2 * np.pi * u2 - np.pi))) < 1e-12
+
+
+def test_initial_field_flavours(oracle):
+    """Initial fields beta_init + beta_init_sigma * xi from the init stream in
+    the FP64 and the FP32 Box-Muller flavour agree with the numpy restatement."""
+    n = 37
+    rng = np.random.default_rng(2)
+    bi = rng.normal(size=n) + 1j * rng.normal(size=n)
+    bs = 0.5 + 0.1 * rng.random(size=n)
+    for f32, tol in ((False, 1e-13), (True, 1e-6)):
+        got = oracle.initial_field(n, bi, bs, 99, 7, f32=f32)
+        ref = bi + bs * npo.site_normals(99, 7, 0, 1, n, f32_flavour=f32)
+        assert np.allclose(got, ref, rtol=0, atol=tol), f32
