@@ -222,6 +222,38 @@ def measure_f64(twmc, torch, steps=2):
             "kernel": kname}
 
 
+def measure_observable_error(twmc, ntraj=256, t_end=T_END):
+    """Error of the FP32 engine's observables against the FP64 engine (the
+    plain FP64 GPU split-step) on the headline workload over its full
+    horizon: the same trajectories (seeds, ids, Philox streams) in both
+    precisions, n, g2 and n_k per frame and site compared in units of the
+    combined standard error (32 trajectory blocks)."""
+    import numpy as np
+    from pincosimulator_gb300 import observables as ob
+
+    nframes = int(round(t_end / (DT * FRAME_STEPS)))
+    per = {}
+    for name, prec in (("f32", twmc.PREC_F32), ("f64", twmc.PREC_F64)):
+        sysd = make_system(twmc, precision=prec)
+        sysd.batch_init(sysd.make_tasks(ntraj, t_start=0.0, t_end=t_end, seed0=424242, id0=1))
+        frames = []
+        t0 = time.perf_counter()
+        for _ in range(nframes):
+            sysd.advance(FRAME_STEPS)
+            sysd.reduce()
+            _, m = sysd.download(field=False, moments=True)
+            o = ob.observables(m, ntraj)
+            frames.append({k: o[k] for k in ("n", "n_se", "g2", "g2_se", "nk", "nk_se", "bm2")})
+        per[name] = ({k: np.stack([f[k] for f in frames]) for k in frames[0]}, time.perf_counter() - t0)
+        sysd.close()
+    c = ob.compare(per["f32"][0], per["f64"][0], frames=slice(0, None))
+    return {"workload": f"headline workload, {ntraj} trajectories, t_end = {t_end:g} ({nframes} frames of "
+                        f"{FRAME_STEPS} steps), same seeds and Philox streams in both precisions",
+            "fp32_vs_fp64": c, "f32_s": round(per["f32"][1], 2), "f64_s": round(per["f64"][1], 2),
+            "units": "max |z| and mean z^2 over frames x sites, z = (FP32 - FP64) / sqrt(SE32^2 + SE64^2); "
+                     "n_site_avg.max_rel_diff = max over frames of |nbar32 - nbar64| / nbar64"}
+
+
 def cpu_baseline(target_s=12.0, threads=None):
     """Oracle port (FP64 restatement, radix-2 FFT, not FFTW) on the host cores:
     a bounded sample of the same workload (trajectories x 250 steps of 64 x 64)."""
@@ -295,6 +327,7 @@ def main():
     ap.add_argument("--no-warm", action="store_true", help="skip the learned warm-start time-to-steady-state leg")
     ap.add_argument("--no-f64", action="store_true", help="skip timing the FP64 mode")
     ap.add_argument("--no-other", action="store_true", help="skip the other configurations")
+    ap.add_argument("--no-obs-err", action="store_true", help="skip the FP32-vs-FP64 observable-error leg")
     ap.add_argument("--ntraj", type=int, default=NTRAJ, help="profiling cases only; the bench line uses 16384")
     args = ap.parse_args()
     rank, world, local = env_rank()
@@ -414,6 +447,9 @@ def main():
     if world == 1 and args.ntraj == NTRAJ and not args.no_f64:
         f64 = measure_f64(twmc, torch)
         f64["fp32_speedup"] = value / f64["value"]
+    obs_err = None
+    if world == 1 and args.ntraj == NTRAJ and not args.no_obs_err:
+        obs_err = measure_observable_error(twmc)
     other = None
     if world == 1 and args.ntraj == NTRAJ and not args.no_other:
         other = measure_other_paths(twmc, torch, clocks.get("sm_mhz") if clocks else None)
@@ -431,7 +467,7 @@ def main():
                              "peak_gbs": hbm, "source": "MEASURED_PEAKS.json" if hbm else None}},
         "issue": issue, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu, "clocks": clocks,
         "trajectories_per_s": value / (NX * NY * (T_END / DT)), "finite": finite,
-        "kernel_ms": kernel_ms, "time_to_steady_state": warm, "fp64_mode": f64,
+        "kernel_ms": kernel_ms, "time_to_steady_state": warm, "fp64_mode": f64, "observable_error": obs_err,
         "other_paths": other,
     }
     print(json.dumps(line), flush=True)

@@ -198,7 +198,8 @@ TWMC_API int twmc_batch_download(twmc_handle* h, double* field, double* moments)
  * reductions, initialisation). */
 TWMC_API int64_t twmc_launch_count(const twmc_handle* h);
 /* Name of the step kernel variant the handle selected: "square_fft_kernel"
- * (register FFT), "ell_kernel<stencil>" / "ell_kernel<table>" (real space,
+ * (register FFT; "square_fft_kernel<fast>" for its compiled-in common run:
+ * FP32, Philox noise, scalar U and F), "ell_kernel<stencil>" / "ell_kernel<table>" (real space,
  * square stencil / Lieb neighbour table), "rowrun_kernel" (square stencil,
  * 4096 sites, FP32 Philox runs), "lieb_cell_kernel" (Lieb lattice, even
  * number of cells), "ell_cluster_pow2_kernel" / "ell_cluster_kernel" (square
@@ -293,11 +294,14 @@ TWMC_API void twmc_hbatch_destroy(twmc_hbatch* b);
  * Limit: n_traj * nx * ny <= 4194304 (the 16 MiB scratch array that every
  * device loading the library holds until the process exits); larger sizes,
  * unsupported shapes and null pointers return TWMC_ERR_INVALID.
- * The first call on a device looks up the scratch array's device address
- * (cudaGetSymbolAddress, with that device current); make that first call
- * before any stream capture. All calls share the one scratch array: calls
- * that overlap on the GPU (different streams, or host threads without
- * ordering) race. The call allocates nothing and does not synchronise. */
+ * Calls outside stream capture look up the scratch array's device address
+ * (cudaGetSymbolAddress, with the device current) and remember it; a call
+ * during capture uses the remembered address, so the first call on a device
+ * -- and the first after a cudaDeviceReset -- must come before any stream
+ * capture (a first call under capture returns TWMC_ERR_CUDA). All calls share
+ * the one scratch array: calls that overlap on the GPU (different streams, or
+ * host threads without ordering) race. The call allocates nothing and does
+ * not synchronise. */
 TWMC_API int twmc_kspace_moments_noalloc(const void* state, int64_t n_traj, int64_t nx, int64_t ny,
                                          int32_t n_blocks, double* moments, void* stream);
 
@@ -366,6 +370,17 @@ TWMC_API int twmc_mlp_fields(const float* rows, int64_t ld, int64_t n_points, co
 /* Philox4x32-10 evaluated on the GPU for n counters (ctr: n x 4, key: 2 words),
  * out: n x 4 words. */
 TWMC_API int twmc_debug_philox(const uint32_t* ctr, size_t n, const uint32_t* key, uint32_t* out);
+
+/* The complex Wiener normals xi of one trajectory exactly as the step kernels
+ * draw them in Philox mode (twmc_system_desc.noise_mode = TWMC_NOISE_PHILOX),
+ * for steps step0 .. step0 + n_steps - 1 of an n_sites lattice, in the run's
+ * precision (TWMC_PREC_F32: the FP32 Box-Muller, widened exactly):
+ * out[(k * n_sites + p) * 2 + {0,1}] = Re, Im of xi at step step0 + k, site p.
+ * The per-step draw of randCMat (TWMCBaseSolver.cpp:285-291), as a device
+ * self-check: a caller can replay a Philox-mode trajectory through any
+ * deterministic-noise implementation with these values. */
+TWMC_API int twmc_debug_wiener(int32_t precision, uint32_t seed, uint64_t id, uint32_t step0, int64_t n_steps,
+                               int64_t n_sites, double* out);
 
 #ifdef __cplusplus
 }

@@ -461,6 +461,7 @@ int advance(twmc_handle* h, int64_t n, bool want_nk, int64_t t0 = 0, int64_t t1 
   if (h->use_fft) {
     ok = h->prec == 0 ? square_launch_f32(h->bx, h->by, a, nparams, h->stream, &h->last_info, &err)
                       : square_launch_f64(h->bx, h->by, a, nparams, h->stream, &h->last_info, &err);
+    if (ok) h->kname = h->last_info.name;  // "square_fft_kernel<fast>" for the compiled-in common run
   } else {
     ok = ell_launch(h->prec, a, h->stream, &h->last_info, &err);
     if (ok && (std::strncmp(h->last_info.name, "ell_cluster", 11) == 0 || std::strcmp(h->last_info.name, "lieb_cell_kernel") == 0 ||
@@ -1146,6 +1147,23 @@ int twmc_debug_philox(const uint32_t* ctr, size_t n, const uint32_t* key, uint32
   std::string err;
   if (!philox_launch(dc.as<uint32_t>(), n, key[0], key[1], dout.as<uint32_t>(), nullptr, &err)) return TWMC_ERR_CUDA;
   if (cudaMemcpy(out, dout.p, n * 16, cudaMemcpyDeviceToHost) != cudaSuccess) return TWMC_ERR_CUDA;
+  return TWMC_OK;
+}
+
+int twmc_debug_wiener(int32_t precision, uint32_t seed, uint64_t id, uint32_t step0, int64_t n_steps,
+                      int64_t n_sites, double* out) {
+  if (precision != TWMC_PREC_F32 && precision != TWMC_PREC_F64) return TWMC_ERR_INVALID;
+  if (n_steps < 0 || n_sites < 1 || (n_steps > 0 && !out)) return TWMC_ERR_INVALID;
+  if (n_steps > (int64_t(1) << 40) / n_sites) return TWMC_ERR_INVALID;
+  const size_t bytes = size_t(n_steps) * size_t(n_sites) * 16;
+  if (bytes == 0) return TWMC_OK;
+  DevBuf dout;
+  if (!dout.ensure(bytes)) return TWMC_ERR_NOMEM;
+  std::string err;
+  if (!wiener_launch(precision == TWMC_PREC_F32 ? 0 : 1, seed, uint32_t(id), step0, n_steps, n_sites,
+                     dout.as<double>(), nullptr, &err))
+    return TWMC_ERR_CUDA;
+  if (cudaMemcpy(out, dout.p, bytes, cudaMemcpyDeviceToHost) != cudaSuccess) return TWMC_ERR_CUDA;
   return TWMC_OK;
 }
 

@@ -89,6 +89,8 @@ bool moments_launch(const MomentArgs& a, cudaStream_t s, std::string* err);
 
 bool fp32_peak(double* tflops, std::string* err);
 
+bool wiener_launch(int prec, uint32_t seed, uint32_t id, uint32_t step0, int64_t nsteps, int64_t n, double* d_out,
+                   cudaStream_t s, std::string* err);
 bool philox_launch(const uint32_t* d_ctr, size_t n, uint32_t k0, uint32_t k1, uint32_t* d_out, cudaStream_t s,
                    std::string* err);
 

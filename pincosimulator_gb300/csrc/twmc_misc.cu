@@ -92,6 +92,31 @@ __global__ void init_kernel(const InitArgs a) {
   }
 }
 
+// Wiener increments of one trajectory exactly as the step kernels draw them
+// in Philox mode: out[(step - step0) * n + p] (interleaved complex, widened
+// to FP64 for an FP32 run), site p taking words (0,1) or (2,3) of call
+// site_ctr(p).
+__global__ void wiener_kernel(int prec, uint32_t seed, uint32_t id, uint32_t step0, int64_t nsteps, int64_t n,
+                              double* out) {
+  const int64_t total = nsteps * n;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < total; i += int64_t(gridDim.x) * blockDim.x) {
+    const int64_t k = i / n, p = i % n;
+    int hi;
+    const uint32_t c0 = site_ctr(p, n, &hi);
+    const u32x4 w = wiener_words(c0, step0 + uint32_t(k), seed, id);
+    const uint32_t u0 = hi ? w.z : w.x, u1 = hi ? w.w : w.y;
+    double2 z;
+    if (prec == 0) {
+      const float2 f = normal_pair(u0, u1, 0.0f);
+      z = make_double2(double(f.x), double(f.y));
+    } else {
+      z = normal_pair(u0, u1, 0.0);
+    }
+    out[2 * i] = z.x;
+    out[2 * i + 1] = z.y;
+  }
+}
+
 __global__ void philox_kernel(const uint32_t* ctr, size_t n, uint32_t k0, uint32_t k1, uint32_t* out) {
   const size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x;
   if (i >= n) return;
@@ -170,6 +195,15 @@ bool fp32_peak(double* tflops, std::string* err) {
   cudaFree(out);
   *tflops = best;
   return best > 0.0;
+}
+
+bool wiener_launch(int prec, uint32_t seed, uint32_t id, uint32_t step0, int64_t nsteps, int64_t n, double* d_out,
+                   cudaStream_t s, std::string* err) {
+  const int64_t total = nsteps * n;
+  if (total <= 0) return true;
+  const int grid = int(std::min<int64_t>((total + 255) / 256, 4096));
+  wiener_kernel<<<grid, 256, 0, s>>>(prec, seed, id, step0, nsteps, n, d_out);
+  return check(cudaGetLastError(), err, "wiener_kernel");
 }
 
 bool philox_launch(const uint32_t* d_ctr, size_t n, uint32_t k0, uint32_t k1, uint32_t* d_out, cudaStream_t s,

@@ -25,20 +25,36 @@ namespace {
 constexpr size_t kNoAllocScratchFloats = size_t(1) << 22;
 static __device__ __align__(256) float g_kspace_scratch[kNoAllocScratchFloats];
 
-// Device address of the scratch array, looked up once per device (with that
-// device current) on the first call.
+// Device address of the scratch array per device (looked up with that device
+// current). The cached address serves calls made during stream capture, where
+// the lookup must not run; calls outside capture look it up again, so a
+// context torn down and recreated (cudaDeviceReset) after an earlier call does
+// not leave a stale address behind.
 std::mutex g_scratch_mu;
 float* g_scratch_ptr[128] = {};
+// Bumped when a device's scratch address changes (its context was recreated):
+// per-plan launch settings made in the old context are redone.
+int g_generation[128] = {};
 
-float* scratch_for_current_device(std::string* err) {
+float* scratch_for_current_device(cudaStream_t s, std::string* err) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= 128) {
     *err = "no current CUDA device";
     return nullptr;
   }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) {
+    cudaGetLastError();
+    *err = "cudaStreamIsCapturing failed";
+    return nullptr;
+  }
   std::lock_guard<std::mutex> lock(g_scratch_mu);
-  if (!g_scratch_ptr[dev]) {
+  if (!g_scratch_ptr[dev] || cap == cudaStreamCaptureStatusNone) {
+    if (cap != cudaStreamCaptureStatusNone) {
+      *err = "first call on this device made during stream capture";
+      return nullptr;
+    }
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_kspace_scratch);
     if (e != cudaSuccess || !p) {
@@ -46,6 +62,7 @@ float* scratch_for_current_device(std::string* err) {
       *err = std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e);
       return nullptr;
     }
+    if (g_scratch_ptr[dev] && g_scratch_ptr[dev] != static_cast<float*>(p)) ++g_generation[dev];
     g_scratch_ptr[dev] = static_cast<float*>(p);
   }
   return g_scratch_ptr[dev];
@@ -127,6 +144,9 @@ __global__ void __launch_bounds__(CTA) kspace_noalloc_kernel(const float2* __res
   }
 }
 
+// Resident CTAs of a plan's kernel on the whole device, per device, found
+// once per context (shared-memory attribute, SM count, occupancy) and cached
+// under the scratch mutex.
 template <class P>
 cudaError_t launch_kspace(const float2* state, int64_t ntraj, float* nk, cudaStream_t s) {
   constexpr int CTA = cta_for<float, P>();
@@ -134,17 +154,36 @@ cudaError_t launch_kspace(const float2* state, int64_t ntraj, float* nk, cudaStr
   using I = PlanInfo<P>;
   const size_t smem = sizeof(float2) * (size_t(I::TW0 + I::TW1) + 2 * size_t(Cfg::XSZ));
   auto fn = kspace_noalloc_kernel<P, CTA>;
-  cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e != cudaSuccess) return e;
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, CTA, smem);
-  if (e != cudaSuccess) return e;
+  static int resident[128] = {};
+  static int generation[128] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 128) return e != cudaSuccess ? e : cudaErrorInvalidDevice;
+  int slots;
+  {
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    if (resident[dev] <= 0 || generation[dev] != g_generation[dev]) {
+      generation[dev] = g_generation[dev];
+      e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+      if (e != cudaSuccess) return e;
+      int sms = 0, per_sm = 0;
+      e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e != cudaSuccess) return e;
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fn, CTA, smem);
+      if (e != cudaSuccess) return e;
+      resident[dev] = sms * std::max(per_sm, 1);
+    }
+    slots = resident[dev];
+  }
   const int64_t groups = (ntraj + Cfg::TPC - 1) / Cfg::TPC;
-  const int grid = int(std::min<int64_t>(groups, int64_t(sms) * std::max(per_sm, 1)));
+  const int grid = int(std::min<int64_t>(groups, int64_t(slots)));
   fn<<<grid, CTA, smem, s>>>(state, ntraj, nk);
-  return cudaGetLastError();
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {  // e.g. the attribute was lost with a recreated context: redo the setup next call
+    std::lock_guard<std::mutex> lock(g_scratch_mu);
+    resident[dev] = 0;
+  }
+  return e;
 }
 
 }  // namespace
@@ -153,16 +192,18 @@ cudaError_t launch_kspace(const float2* state, int64_t ntraj, float* nk, cudaStr
 extern "C" int twmc_kspace_moments_noalloc(const void* state, int64_t n_traj, int64_t nx, int64_t ny,
                                             int32_t n_blocks, double* moments, void* stream) {
   using namespace twmc;
-  if (!state || !moments || n_traj < 1 || nx < 1 || ny < 1 || n_blocks < 1 || n_blocks > 65535)
-    return TWMC_ERR_INVALID;
+  if (!state || !moments || n_traj < 1 || n_blocks < 1 || n_blocks > 65535) return TWMC_ERR_INVALID;
+  // the compiled plans have at most 4096 sites: bound both sides before any
+  // arithmetic on them
+  if (nx < 1 || ny < 1 || nx > 4096 || ny > 4096 || nx * ny > 4096) return TWMC_ERR_INVALID;
   auto lg = [](int64_t v) { int b = 0; while ((int64_t(1) << b) < v) ++b; return (int64_t(1) << b) == v ? b : -1; };
   const int bx = lg(nx), by = lg(ny);
   const int64_t n = nx * ny;
   if (n_traj > int64_t(kNoAllocScratchFloats) / n) return TWMC_ERR_INVALID;  // beyond the scratch array
-  std::string err;
-  float* nk = scratch_for_current_device(&err);
-  if (!nk) return TWMC_ERR_CUDA;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::string err;
+  float* nk = scratch_for_current_device(s, &err);
+  if (!nk) return TWMC_ERR_CUDA;
   const float2* st = static_cast<const float2*>(state);
   cudaError_t e = cudaErrorInvalidValue;
   bool shape_ok = true;

@@ -57,7 +57,7 @@ bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo*
   const int64_t groups = (a.ntraj + Cfg::TPC - 1) / Cfg::TPC;
   const int grid = int(std::min<int64_t>(groups, int64_t(sms) * per_sm));
   if (info) {
-    info->name = "square_fft_kernel";
+    info->name = FAST ? "square_fft_kernel<fast>" : "square_fft_kernel";
     info->cta = CTA;
     info->grid = grid;
     info->smem = smem;

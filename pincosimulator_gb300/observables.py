@@ -87,3 +87,57 @@ def time_to_steady_state(times: np.ndarray, nbar: np.ndarray, nbar_se: np.ndarra
         if dev[k] <= tol[k] and np.all(dev[nxt] <= 2.0 * tol[nxt]):
             return float(times[k]), n_inf
     return float(times[-1]), n_inf
+
+
+def frame_observables(frames: np.ndarray, nblocks: int = 32) -> dict:
+    """The same estimators from raw fields (T, F, N) complex, blocked like the
+    engine's moment blocks (block b = trajectories [b T / B, (b + 1) T / B))."""
+    x = np.asarray(frames)
+    T = x.shape[0]
+    ab2 = np.abs(x) ** 2
+    edges = (np.arange(nblocks + 1) * T) // nblocks
+    m = np.zeros((x.shape[1], nblocks, x.shape[2], 3))
+    for b in range(nblocks):
+        s = slice(edges[b], edges[b + 1])
+        m[:, b, :, 0] = ab2[s].sum(0)
+        m[:, b, :, 1] = (ab2[s] ** 2).sum(0)
+    return observables(m, T)
+
+
+def _z(a, sa, b, sb):
+    with np.errstate(divide="ignore", invalid="ignore"):
+        return (np.asarray(a) - np.asarray(b)) / np.sqrt(np.asarray(sa) ** 2 + np.asarray(sb) ** 2)
+
+
+def compare(a: dict, b: dict, frames=slice(1, None), keys=("n", "g2", "nk")) -> dict:
+    """Difference of two ensembles' observables in units of their combined
+    standard error, z = (a - b) / sqrt(se_a^2 + se_b^2), per frame and site
+    (frames: which save frames; frame 0 is the shared initial state).
+
+    For each observable: max |z| and the mean of z^2 over frames and sites,
+    and for n also the site-averaged density (its SE from the batch means of
+    the site-averaged block densities). For independent ensembles of the same
+    process z is close to N(0, 1): mean z^2 about 1. Ensembles sharing noise
+    streams are positively correlated, so their z is smaller."""
+    out = {}
+    for k in keys:
+        if k not in a or k not in b:
+            continue
+        z = _z(a[k][frames], a[k + "_se"][frames], b[k][frames], b[k + "_se"][frames])
+        z = z[np.isfinite(z)]
+        if z.size == 0:
+            continue
+        out[k] = {"max_abs_z": float(np.abs(z).max()), "mean_z2": float(np.mean(z ** 2)), "count": int(z.size)}
+
+    def nbar(o):
+        bm = o["bm2"][frames].mean(axis=-1)  # (F, B) site-averaged block <|a|^2>
+        B = bm.shape[-1]
+        return o["n"][frames].mean(axis=-1), bm.std(axis=-1, ddof=1) / np.sqrt(B)
+
+    na, sa = nbar(a)
+    nb, sb = nbar(b)
+    zb = _z(na, sa, nb, sb)
+    out["n_site_avg"] = {"max_abs_z": float(np.abs(zb).max()), "mean_z2": float(np.mean(zb ** 2)),
+                         "count": int(zb.size),
+                         "max_rel_diff": float(np.max(np.abs(na - nb) / np.maximum(np.abs(nb), 1e-300)))}
+    return out

@@ -29,7 +29,7 @@ EXPORTED = [
     "twmc_version", "twmc_create", "twmc_run", "twmc_set_noise_buffer", "twmc_progress", "twmc_last_error",
     "twmc_destroy", "twmc_batch_init", "twmc_batch_advance", "twmc_batch_reduce", "twmc_sync",
     "twmc_batch_download", "twmc_launch_count", "twmc_kernel_name", "twmc_stream", "twmc_measure_fp32_peak",
-    "twmc_kspace_moments_noalloc", "twmc_debug_philox",
+    "twmc_kspace_moments_noalloc", "twmc_debug_philox", "twmc_debug_wiener",
     "twmc_hbatch_create", "twmc_hbatch_run", "twmc_hbatch_sync", "twmc_hbatch_moments", "twmc_hbatch_state",
     "twmc_hbatch_plan", "twmc_hbatch_last_error", "twmc_hbatch_launch_count", "twmc_hbatch_destroy",
     "twmc_hbatch_set_init", "twmc_hbatch_field_moments", "twmc_hbatch_total_sites", "twmc_hbatch_stream",
@@ -113,6 +113,8 @@ def load(path: Optional[str] = None):
     lib.twmc_kernel_name.argtypes = [C.c_void_p]
     lib.twmc_kernel_name.restype = C.c_char_p
     lib.twmc_debug_philox.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p, C.c_void_p]
+    lib.twmc_debug_wiener.argtypes = [C.c_int32, C.c_uint32, C.c_uint64, C.c_uint32, C.c_int64, C.c_int64,
+                                      C.c_void_p]
     lib.twmc_stream.argtypes = [C.c_void_p]
     lib.twmc_stream.restype = C.c_void_p
     lib.twmc_measure_fp32_peak.argtypes = [C.POINTER(C.c_double)]
@@ -591,4 +593,16 @@ def debug_philox(ctr: np.ndarray, key) -> np.ndarray:
     rc = lib.twmc_debug_philox(ctr.ctypes.data, ctr.shape[0], k.ctypes.data, out.ctypes.data)
     if rc != OK:
         raise TWMCError(rc, "twmc_debug_philox failed")
+    return out
+
+
+def debug_wiener(precision: int, seed: int, tid: int, n_steps: int, n_sites: int, step0: int = 0) -> np.ndarray:
+    """Philox-mode Wiener normals of one trajectory as the step kernels draw
+    them: (n_steps, n_sites) complex128."""
+    lib = load()
+    out = np.zeros((n_steps, n_sites), dtype=np.complex128)
+    rc = lib.twmc_debug_wiener(precision, seed & 0xFFFFFFFF, tid, step0 & 0xFFFFFFFF, n_steps, n_sites,
+                               out.ctypes.data)
+    if rc != OK:
+        raise TWMCError(rc, "twmc_debug_wiener failed")
     return out

@@ -65,3 +65,15 @@ def check(res, refs, prec):
         fw = ref["frames_written"]
         e = rel_err(res["frames"][k, :fw], ref["frames"][:fw])
         assert e < tol, f"traj {k}: frames rel err {e:.3e} > {tol}"
+
+
+def philox_ref(orc, prec, seed, tid, steps, n, **run):
+    """Oracle run of one Philox-mode trajectory: FP64 runs draw the oracle's
+    own FP64 Philox stream; FP32 runs replay the device's normals
+    (twmc_debug_wiener: the same Philox words through the FP32 Box-Muller with
+    hardware log / sin / cos) in deterministic-noise mode, so the comparison
+    holds the step arithmetic to the FP32 parity tolerance."""
+    if prec == twmc.PREC_F64:
+        return orc.base_run(**run, seed=seed, tid=tid, noise="philox64")
+    xi = twmc.debug_wiener(twmc.PREC_F32, seed, tid, steps, n)
+    return orc.base_run(**run, xi=xi)

@@ -1,0 +1,153 @@
+"""Long-horizon checks of the FP32 engine and a direct oracle check of the
+exact step-kernel instantiation the headline workload runs.
+
+* The headline kernel: 64x64, per-site omega disorder, Philox noise, FP32 --
+  the compiled-in fast instantiation of the register-FFT kernel -- against the
+  FP64 oracle fed the device's own Wiener normals, 500 steps, 1e-5.
+* Ensemble agreement over 10^4 steps (t = 20 at dt = 0.002, the
+  TWMCBaseSolver.cpp:232-266 loop): n, g2 and n_k per frame and site of the
+  FP32 engine against the FP64 engine on the same noise streams and on
+  independent ones, and against an ensemble of oracle trajectories, in units
+  of the combined standard error.
+"""
+import os
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+import pytest
+
+from pincosimulator_gb300 import observables as obs
+from pincosimulator_gb300 import twmc
+
+from gpu_util import rel_err
+
+pytestmark = pytest.mark.gpu
+
+# the headline workload's parameters (2-D, omega_i = -0.5 + N(0, 0.2^2), U = 0.2, F = 2)
+J, GAMMA, U, F, DT = 1.0, 1.0, 0.2, 2.0, 0.002
+
+
+def _system(nx, ny, prec, frame_steps, nb=32):
+    return twmc.System(nx=nx, ny=ny, J=J, gamma=GAMMA, dt=DT, frame_steps=frame_steps,
+                       omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=U, F=F, beta_init=0.0,
+                       beta_init_sigma=0.5, precision=prec, n_moment_blocks=nb)
+
+
+def test_device_normals_are_the_philox_stream(built_lib, oracle):
+    """twmc_debug_wiener draws the oracle's Philox stream: FP64 normals to
+    1e-14, FP32 normals (hardware log / sin / cos) to a few 1e-6."""
+    n, steps = 4096, 4
+    for prec, f32, tol in ((twmc.PREC_F64, False, 1e-14), (twmc.PREC_F32, True, 2e-5)):
+        xi = twmc.debug_wiener(prec, 77, 5, steps, n, step0=100)
+        for k in range(steps):
+            ref = oracle.site_normals(77, 5, 100 + k, 0, n, f32=f32)
+            d = np.abs(xi[k] - ref) / np.maximum(1.0, np.abs(ref))
+            assert d.max() < tol, (prec, k, d.max())
+
+
+def test_headline_kernel_matches_oracle(built_lib, oracle):
+    """The exact kernel of the headline workload (64x64, per-site omega, FP32
+    Philox, the fast instantiation) for 500 steps (two 250-step frames) from
+    device-drawn initial fields: every frame and the final field of each
+    trajectory equal the FP64 oracle's (TWMCBaseSolver.cpp:232-266) fed the
+    same Wiener normals (twmc_debug_wiener) and the drawn omega realisation,
+    within 1e-5 relative."""
+    nx = ny = 64
+    n = nx * ny
+    ntraj, fs, nfr = 3, 250, 2
+    steps = fs * nfr
+    sysd = _system(nx, ny, twmc.PREC_F32, fs)
+    tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=steps * DT, seed0=901, id0=40)
+    res = sysd.run(tasks, frames=True, realizations=True)
+    kernel = sysd.kernel_name
+    sysd.close()
+    assert kernel == "square_fft_kernel<fast>", kernel
+    assert (res["status"] == 0).all()
+    for k in range(ntraj):
+        xi = twmc.debug_wiener(twmc.PREC_F32, 901 + k, 40 + k, steps, n)
+        ref = oracle.base_run(nx, ny, J, GAMMA, DT, 0.0, steps * DT, fs, nfr + 1, True, res["omega_realization"][k],
+                              U, F, res["frames"][k, 0], xi=xi)
+        assert ref["steps"] == steps
+        assert res["frames_written"][k] == ref["frames_written"] == nfr + 1
+        e = rel_err(res["frames"][k], ref["frames"])
+        assert e < 1e-5, f"traj {k}: frames rel err {e:.2e}"
+        e = rel_err(res["final"][k], ref["final"])
+        assert e < 1e-5, f"traj {k}: final rel err {e:.2e}"
+
+
+def _ensemble(nx, ny, prec, ntraj, seed0, t_end, fs):
+    sysd = _system(nx, ny, prec, fs)
+    tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=t_end, seed0=seed0, id0=1)
+    res = sysd.run(tasks, frames=False, final=False, moments=True)
+    sysd.close()
+    return obs.observables(res["moments"], ntraj)
+
+
+LONG = dict(nx=16, ny=16, ntraj=2048, t_end=20.0, fs=250)  # 10^4 steps, 40 frames + the initial one
+
+
+@pytest.fixture(scope="module")
+def long_runs(built_lib):
+    p = LONG
+    o32 = _ensemble(p["nx"], p["ny"], twmc.PREC_F32, p["ntraj"], 11, p["t_end"], p["fs"])
+    o64 = _ensemble(p["nx"], p["ny"], twmc.PREC_F64, p["ntraj"], 11, p["t_end"], p["fs"])
+    o64i = _ensemble(p["nx"], p["ny"], twmc.PREC_F64, p["ntraj"], 500011, p["t_end"], p["fs"])
+    return o32, o64, o64i
+
+
+def test_long_run_fp32_vs_fp64_same_streams(long_runs):
+    """FP32 state / FFT against the FP64 mode on the same Philox streams over
+    10^4 steps: the observables agree far inside their standard errors (the
+    FP32 error reported in SE units)."""
+    o32, o64, _ = long_runs
+    c = obs.compare(o32, o64)
+    print("FP32 vs FP64, same streams:", c)
+    assert np.isfinite(o32["n"]).all() and np.isfinite(o64["n"]).all()
+    for k in ("n", "g2", "nk", "n_site_avg"):
+        assert c[k]["max_abs_z"] < 3.0, (k, c[k])
+        assert c[k]["mean_z2"] < 0.5, (k, c[k])
+
+
+def test_long_run_fp32_vs_independent_fp64(long_runs):
+    """FP32 against an FP64 ensemble on independent streams: the same
+    distribution, so z ~ N(0, 1) per frame and site (10240 values per
+    observable): mean z^2 near 1, no |z| above 5."""
+    o32, _, o64i = long_runs
+    c = obs.compare(o32, o64i)
+    print("FP32 vs FP64, independent streams:", c)
+    for k in ("n", "g2", "nk"):
+        assert c[k]["max_abs_z"] < 5.5, (k, c[k])
+        assert 0.6 < c[k]["mean_z2"] < 1.6, (k, c[k])
+    assert c["n_site_avg"]["max_abs_z"] < 4.5, c["n_site_avg"]
+
+
+def test_long_run_against_oracle_ensemble(built_lib, oracle, long_runs):
+    """256 trajectories of the FP64 oracle (Philox FP64 noise, the engine's
+    own initial fields and omega realisations) over the same 10^4 steps
+    against the engine's FP32 ensemble: n and g2 within their standard
+    errors at every frame and site."""
+    p = LONG
+    nx, ny, fs, t_end = p["nx"], p["ny"], p["fs"], p["t_end"]
+    n = nx * ny
+    nt = 256
+    sysd = _system(nx, ny, twmc.PREC_F64, fs)
+    tasks = sysd.make_tasks(nt, t_start=0.0, t_end=DT * fs, seed0=11, id0=1)
+    init = sysd.run(tasks, frames=True, realizations=True)
+    sysd.close()
+    nfr = int(round(t_end / (DT * fs))) + 1
+
+    def one(k):
+        r = oracle.base_run(nx, ny, J, GAMMA, DT, 0.0, t_end, fs, nfr, True, init["omega_realization"][k], U, F,
+                            init["frames"][k, 0], seed=11 + k, tid=1 + k, noise="philox64")
+        assert r["frames_written"] == nfr
+        return r["frames"]
+
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
+        fr = np.stack(list(ex.map(one, range(nt))))
+    o_orc = obs.frame_observables(fr, 32)
+    o32, _, _ = long_runs
+    c = obs.compare(o32, o_orc, keys=("n", "g2"))
+    print("FP32 engine vs oracle ensemble:", c)
+    for k in ("n", "g2", "n_site_avg"):
+        assert c[k]["max_abs_z"] < 5.0, (k, c[k])
+        assert c[k]["mean_z2"] < 1.6, (k, c[k])

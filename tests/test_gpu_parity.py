@@ -9,7 +9,7 @@ import pytest
 
 from pincosimulator_gb300 import twmc
 
-from gpu_util import check, lieb_case, rel_err, square_case
+from gpu_util import check, lieb_case, philox_ref, rel_err, square_case
 
 pytestmark = pytest.mark.gpu
 
@@ -57,8 +57,8 @@ def test_cluster_stencil_parity(built_lib, oracle, shape, kernel):
                                               ((256, 64), True)])
 def test_cluster_pow2_philox(built_lib, oracle, shape, site_omega):
     """Philox-mode runs on the fast power-of-two cluster kernel (noise and
-    scalar U, F compiled in; omega per site allowed) against the oracle's
-    Philox stream (FP32 Box-Muller flavour)."""
+    scalar U, F compiled in; omega per site allowed) against the oracle fed
+    the device's Philox normals, 1e-5."""
     nx, ny = shape
     n = nx * ny
     ntraj, steps, dt = 2, 100, 0.005
@@ -75,9 +75,10 @@ def test_cluster_pow2_philox(built_lib, oracle, shape, site_omega):
     sysd.close()
     assert kernel == "ell_cluster_pow2_kernel"
     for k in range(ntraj):
-        ref = oracle.base_run(nx, ny, 1.0, 1.0, dt, 0.0, steps * dt, 50, 3, True, omega, 0.2, 1.5, beta0[k],
-                              seed=seeds[k], tid=9 + k, noise="philox32")
-        assert rel_err(res["final"][k], ref["final"]) < 1e-4
+        ref = philox_ref(oracle, twmc.PREC_F32, seeds[k], 9 + k, steps, n, nx=nx, ny=ny, J=1.0, gamma=1.0, dt=dt,
+                         t_start=0.0, t_end=steps * dt, frame_steps=50, n_frames=3, store_initial=True, omega=omega,
+                         U=0.2, F=1.5, beta0=beta0[k])
+        assert rel_err(res["final"][k], ref["final"]) < 1e-5
 
 
 @pytest.mark.parametrize("shape,site_omega", [((64, 64), True), ((64, 64), False), ((1, 4096), True),
@@ -85,7 +86,7 @@ def test_cluster_pow2_philox(built_lib, oracle, shape, site_omega):
 def test_rowrun_philox(built_lib, oracle, shape, site_omega):
     """FP32 Philox runs of the real-space stencil on 4096 sites take the
     row-run kernel (four sites along a row per thread; ny = 4 makes a run a
-    whole row) and agree with the oracle's Philox stream."""
+    whole row) and agree with the oracle fed the device's Philox normals."""
     nx, ny = shape
     n = nx * ny
     ntraj, steps, dt = 2, 60, 0.005
@@ -102,9 +103,10 @@ def test_rowrun_philox(built_lib, oracle, shape, site_omega):
     sysd.close()
     assert kernel == "rowrun_kernel"
     for k in range(ntraj):
-        ref = oracle.base_run(nx, ny, 1.0, 1.0, dt, 0.0, steps * dt, 50, 2, True, omega, 0.2, 1.5, beta0[k],
-                              seed=seeds[k], tid=3 + k, noise="philox32")
-        assert rel_err(res["final"][k], ref["final"]) < 1e-4
+        ref = philox_ref(oracle, twmc.PREC_F32, seeds[k], 3 + k, steps, n, nx=nx, ny=ny, J=1.0, gamma=1.0, dt=dt,
+                         t_start=0.0, t_end=steps * dt, frame_steps=50, n_frames=2, store_initial=True, omega=omega,
+                         U=0.2, F=1.5, beta0=beta0[k])
+        assert rel_err(res["final"][k], ref["final"]) < 1e-5
 
 
 def test_cluster_per_site_parameters(built_lib, oracle):

@@ -53,3 +53,22 @@ def test_time_to_steady_state():
     assert abs(ninf - 2.0) < 1e-3
     # 2 e^{-t/3} <= 0.01 from t = 3 ln 200 = 15.9 on
     assert 15.5 <= ts <= 16.5
+
+
+def test_compare_reports_bias_in_standard_errors():
+    """compare(): two samples of one distribution give z ~ N(0, 1); a bias of
+    five standard errors planted in one ensemble's fields shows up as |z| of
+    about five in n and in the site-averaged density."""
+    rng = np.random.default_rng(4)
+    T, F, N = 1024, 6, 32
+    a = 0.7 * (rng.normal(size=(T, F, N)) + 1j * rng.normal(size=(T, F, N)))
+    b = 0.7 * (rng.normal(size=(T, F, N)) + 1j * rng.normal(size=(T, F, N)))
+    oa, ob_ = ob.frame_observables(a), ob.frame_observables(b)
+    c = ob.compare(oa, ob_, keys=("n", "g2"))
+    assert 0.5 < c["n"]["mean_z2"] < 1.6 and c["n"]["max_abs_z"] < 4.5
+    assert 0.5 < c["g2"]["mean_z2"] < 1.6
+    se = float(np.median(oa["n_se"]))
+    biased = ob.frame_observables(np.sqrt(1.0 + 5.0 * se / (np.abs(b) ** 2).mean()) * b)
+    c2 = ob.compare(oa, biased, keys=("n",))
+    assert c2["n"]["mean_z2"] > 10.0
+    assert c2["n_site_avg"]["max_abs_z"] > 20.0

@@ -37,14 +37,19 @@ def library_moments(nx, ny, ntraj, seed, nblocks):
     return field, moments
 
 
-def test_noalloc_matches_library_path_twice(built_lib):
+@pytest.mark.parametrize("nx,ny,runs", [
+    (64, 64, ((600, 11), (97, 23))),    # one trajectory per CTA
+    (32, 32, ((1001, 5), (333, 6))),    # several trajectories per CTA
+    (16, 16, ((2049, 7), (37, 8))),     # n_traj not a multiple of the trajectories per CTA
+    (1, 256, ((777, 9), (65, 10))),     # 1-D chain plan
+])
+def test_noalloc_matches_library_path_twice(built_lib, nx, ny, runs):
     torch = pytest.importorskip("torch")
     if not torch.cuda.is_available():
         pytest.skip("needs a CUDA device")
     lib = twmc.load()
-    nx = ny = 64
     nb = 16
-    for ntraj, seed in ((600, 11), (97, 23)):
+    for ntraj, seed in runs:
         field, ref = library_moments(nx, ny, ntraj, seed, nb)
         # the caller's own device buffers: complex64 state, FP64 output
         state = torch.from_numpy(field.astype(np.complex64)).cuda()
@@ -58,6 +63,35 @@ def test_noalloc_matches_library_path_twice(built_lib):
         assert np.isfinite(got).all()
         err = np.abs(got - ref).max() / np.abs(ref).max()
         assert err < TOL, f"{ntraj} trajectories: relative error {err:.3e}"
+
+
+def test_noalloc_more_blocks_than_trajectories(built_lib):
+    """n_blocks > n_traj: block b holds trajectories [b T / B, (b + 1) T / B),
+    so the blocks without a trajectory are exactly zero and the block sums
+    equal the library path's (which clamps the block count to T)."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("needs a CUDA device")
+    lib = twmc.load()
+    nx = ny = 32
+    ntraj, nb = 5, 12
+    field, ref = library_moments(nx, ny, ntraj, 31, nb)
+    assert np.all(ref[ntraj:] == 0)  # the library path fills min(n_blocks, n_traj) blocks
+    ref = ref[:ntraj]
+    state = torch.from_numpy(field.astype(np.complex64)).cuda()
+    out = torch.full((nb, nx * ny, 3), float("nan"), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+    rc = lib.twmc_kspace_moments_noalloc(C.c_void_p(state.data_ptr()), ntraj, nx, ny, nb,
+                                         C.c_void_p(out.data_ptr()), None)
+    assert rc == twmc.OK
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    cnt = np.diff((np.arange(nb + 1) * ntraj) // nb)
+    assert np.all(got[cnt == 0] == 0.0)
+    full = got[cnt > 0]
+    assert full.shape == ref.shape
+    err = np.abs(full - ref).max() / np.abs(ref).max()
+    assert err < TOL, f"relative error {err:.3e}"
 
 
 def test_noalloc_rejects_sizes_beyond_the_scratch(built_lib):
@@ -74,3 +108,8 @@ def test_noalloc_rejects_sizes_beyond_the_scratch(built_lib):
     rc = lib.twmc_kspace_moments_noalloc(C.c_void_p(state.data_ptr()), 2, 48, 64, 1, C.c_void_p(out.data_ptr()),
                                          None)
     assert rc == twmc.ERR_INVALID
+    # sides beyond any compiled plan are rejected before any arithmetic on them
+    for nx, ny in ((1 << 40, 1 << 40), (-1, 64), (8192, 1), (128, 64)):
+        rc = lib.twmc_kspace_moments_noalloc(C.c_void_p(state.data_ptr()), 1, nx, ny, 1, C.c_void_p(out.data_ptr()),
+                                             None)
+        assert rc == twmc.ERR_INVALID, (nx, ny)
