@@ -96,8 +96,8 @@ void normal_pair_f64(uint32_t a, uint32_t b, double* z0, double* z1) {
 // (one correctly rounded float fma each), the transcendental part in FP64.
 void normal_pair_f32(uint32_t a, uint32_t b, double* z0, double* z1) {
   const float u1 = std::fma(float(a), 0x1p-32f, 0x1p-33f);
-  const float u2 = std::fma(float(b), 0x1p-32f, 0x1p-33f);
-  const float th = std::fma(u2, float(2.0 * M_PI), -float(M_PI));
+  // th = 2 pi u2 - pi with u2 = float(b) 2^-32 + 2^-33, as one FP32 fma of float(b)
+  const float th = std::fma(float(b), float(2.0 * M_PI * 0x1p-32), float(2.0 * M_PI * 0x1p-33 - M_PI));
   const double r = std::sqrt(std::max(0.0, -2.0 * std::log(double(u1))));
   *z0 = r * std::cos(double(th));
   *z1 = r * std::sin(double(th));

@@ -61,9 +61,10 @@ def site_normals(seed: int, tid: int, step: int, stream: int, n: int, f32_flavou
         # float(a) rounds to nearest; fma(x, 2^-32, 2^-33) is exact up to one
         # float rounding, reproduced here by rounding the exact double value.
         u1 = (a.astype(np.float32).astype(np.float64) * 2.0**-32 + 2.0**-33).astype(np.float32).astype(np.float64)
-        u2 = (b.astype(np.float32).astype(np.float64) * 2.0**-32 + 2.0**-33).astype(np.float32)
-        th = (u2.astype(np.float64) * np.float64(np.float32(2 * np.pi)) - np.float64(np.float32(np.pi)))
-        th = th.astype(np.float32).astype(np.float64)
+        # th = fma(float(b), float(2 pi 2^-32), float(2 pi 2^-33 - pi)) in FP32
+        c1 = np.float64(np.float32(2 * np.pi * 2.0**-32))
+        c2 = np.float64(np.float32(2 * np.pi * 2.0**-33 - np.pi))
+        th = (b.astype(np.float32).astype(np.float64) * c1 + c2).astype(np.float32).astype(np.float64)
         r = np.sqrt(np.maximum(0.0, -2.0 * np.log(u1)))
     else:
         u1 = (a + 0.5) * 2.0**-32

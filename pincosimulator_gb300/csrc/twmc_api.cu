@@ -419,6 +419,7 @@ int advance(twmc_handle* h, int64_t n, bool want_nk, int64_t t0 = 0, int64_t t1 
   for (int k = 0; k < 3; ++k) { a.f_par[2 * k] = float(sc[k][0]); a.f_par[2 * k + 1] = float(sc[k][1]); }
   a.f_dt = float(a.dt);
   a.f_dt4 = float(a.dt4);
+  a.f_kn = float(-2.0 * M_LN2 * h->gamma * h->dt / 4.0);
   a.noise_mode = h->noise_mode;
   a.noise_traj_stride = h->noise_steps * h->nsites;
   a.noise = at(h->d_noise.p, size_t(a.noise_traj_stride) * c2);

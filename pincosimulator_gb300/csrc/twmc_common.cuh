@@ -136,17 +136,33 @@ __host__ __device__ __forceinline__ u32x4 wiener_words(uint32_t pair, uint32_t s
   return philox4x32_10(u32x4{pair, step, id, seed}, kWienerKey0, kWienerKey1);
 }
 
-// Box-Muller, FP32: u = fma(float(w), 2^-32, 2^-33) in (0, 1]; angle in [-pi, pi).
-__device__ __forceinline__ float2 normal_pair(uint32_t a, uint32_t b, float) {
+// Box-Muller, FP32, scaled by s: s (r cos th, r sin th) with r = sqrt(-2 ln u1),
+// u1 = fma(float(a), 2^-32, 2^-33) in (0, 1], th = 2 pi u2 - pi, u2 the same
+// map of b. The radius is computed as sqrt(kn log2 u1) with kn = -2 ln(2) s^2
+// (hardware log2 and square root), so a scale costs nothing; th is one FMA
+// of float(b).
+__device__ __forceinline__ float lg2_approx(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+__device__ __forceinline__ float sqrt_approx(float x) {
+  float y;
+  asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+constexpr float kNegTwoLn2 = -1.38629436111989061883f;  // -2 ln 2: kn of the unscaled normals
+__device__ __forceinline__ float2 scaled_normal_pair(uint32_t a, uint32_t b, float kn) {
   const float u1 = __fmaf_rn(__uint2float_rn(a), 0x1p-32f, 0x1p-33f);
-  const float u2 = __fmaf_rn(__uint2float_rn(b), 0x1p-32f, 0x1p-33f);
-  const float th = __fmaf_rn(u2, 6.28318530717958647692f, -3.14159265358979323846f);
-  // r = sqrt(-2 ln u1) with the hardware log2 / reciprocal square root
-  const float r2 = fmaxf(-2.0f * __logf(u1), 0.0f);
-  const float r = r2 * rsqrtf(fmaxf(r2, 1e-30f));
-  float s, c;
-  __sincosf(th, &s, &c);
-  return make_float2(r * c, r * s);
+  // 2 pi (float(b) 2^-32 + 2^-33) - pi
+  const float th = __fmaf_rn(__uint2float_rn(b), 1.46291807926715968e-9f, -3.14159265285833420f);
+  const float r = sqrt_approx(fmaxf(kn * lg2_approx(u1), 0.0f));
+  float sn, cs;
+  __sincosf(th, &sn, &cs);
+  return make_float2(r * cs, r * sn);
+}
+__device__ __forceinline__ float2 normal_pair(uint32_t a, uint32_t b, float) {
+  return scaled_normal_pair(a, b, kNegTwoLn2);
 }
 
 // Box-Muller, FP64: u = (w + 1/2) 2^-32.

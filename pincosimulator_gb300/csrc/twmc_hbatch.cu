@@ -354,6 +354,7 @@ void fill_args(const twmc_hbatch* b, size_t i, StepArgs* a) {
   for (int k = 0; k < 6; ++k) a->f_par[k] = float(sc[k]);
   a->f_dt = float(a->dt);
   a->f_dt4 = float(a->dt4);
+  a->f_kn = float(-2.0 * M_LN2 * d.gamma * d.dt / 4.0);
   a->noise_mode = TWMC_NOISE_PHILOX;
   a->nsites = d.nx * d.ny;
   a->nx = d.nx;

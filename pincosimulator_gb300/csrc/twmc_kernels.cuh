@@ -40,6 +40,7 @@ struct StepArgs {
   double rsl_s[2], iU_s[2], iF_s[2];
   double dt, dt4;
   float f_par[6];         // FP32 copies of rsl_s, iU_s, iF_s
+  float f_kn;             // -2 ln(2) gamma dt / 4: FP32 Wiener terms come pre-scaled (scaled_normal_pair)
   float f_dt, f_dt4;      // (FP32 kernels read these: a double-to-float conversion
   float f_J;              //  re-done inside a loop runs on the narrow FP64 pipe)
   // noise
@@ -116,6 +117,27 @@ __device__ __forceinline__ T local_update_fused(T b, T hdt, T rsl, T iU, T iF, R
   nb = cmake<T>(nb.x + hdt.x + dt * iF.x, nb.y + hdt.y + dt * iF.y);
   return cmake<T>(nb.x + dt4 * xi.x, nb.y + dt4 * xi.y);
 }
+
+// Wiener term of one Philox word pair in the form the updates add it: FP32
+// kernels get sqrt(gamma dt / 4) xi directly from the scaled Box-Muller and
+// add it with unit scale (Wiener<float>::scale = 1); FP64 kernels get xi and
+// scale it by dt4 in the update. Deterministic-noise buffer values take the
+// same form.
+template <typename R> struct Wiener;
+template <> struct Wiener<float> {
+  static __device__ __forceinline__ float2 term(uint32_t a, uint32_t b, const StepArgs& s) {
+    return scaled_normal_pair(a, b, s.f_kn);
+  }
+  static __device__ __forceinline__ float2 buffer(float2 xi, float dt4) { return make_float2(dt4 * xi.x, dt4 * xi.y); }
+  static __device__ __forceinline__ float scale(float) { return 1.0f; }
+};
+template <> struct Wiener<double> {
+  static __device__ __forceinline__ double2 term(uint32_t a, uint32_t b, const StepArgs&) {
+    return normal_pair(a, b, 0.0);
+  }
+  static __device__ __forceinline__ double2 buffer(double2 xi, double) { return xi; }
+  static __device__ __forceinline__ double scale(double dt4) { return dt4; }
+};
 
 // ------------------------------------------------------------------------
 // compile-time plan helpers (P = generated Plan_bx_by)
@@ -433,12 +455,12 @@ struct SquareGroup {
         if (FAST || a.noise_mode == 0) {
           const int p = pos_thr[0] | I::pos_reg(0, s_lo);  // p < N/2
           const u32x4 w = wiener_words(uint32_t(p), gstep, seed, id);
-          xi_lo = normal_pair(w.x, w.y, R(0));
-          xi_hi = normal_pair(w.z, w.w, R(0));
+          xi_lo = Wiener<R>::term(w.x, w.y, a);
+          xi_hi = Wiener<R>::term(w.z, w.w, a);
         } else {
           const T* nz = noise_tr + (int64_t(gstep)) * N;
-          xi_lo = nz[pos_thr[0] | I::pos_reg(0, s_lo)];
-          xi_hi = nz[pos_thr[0] | I::pos_reg(0, s_hi)];
+          xi_lo = Wiener<R>::buffer(nz[pos_thr[0] | I::pos_reg(0, s_lo)], dt4);
+          xi_hi = Wiener<R>::buffer(nz[pos_thr[0] | I::pos_reg(0, s_hi)], dt4);
         }
         T r_lo = rsl_s, r_hi = rsl_s, u_lo = iU_s, u_hi = iU_s, f_lo = iF_s, f_hi = iF_s;
         {
@@ -451,11 +473,11 @@ struct SquareGroup {
         constexpr std::integral_constant<int, s_lo> SL{};
         constexpr std::integral_constant<int, s_hi> SH{};
         if constexpr (sizeof(R) == 4) {  // dt is folded into the k-space table
-          bset(SL, local_update_fused(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, dt4, xi_lo));
-          bset(SH, local_update_fused(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, dt4, xi_hi));
+          bset(SL, local_update_fused(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo));
+          bset(SH, local_update_fused(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi));
         } else {
-          bset(SL, local_update(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, dt4, xi_lo));
-          bset(SH, local_update(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, dt4, xi_hi));
+          bset(SL, local_update(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo));
+          bset(SH, local_update(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi));
         }
       });
     }
@@ -655,12 +677,12 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
         T xi_lo, xi_hi;
         if (FAST || a.noise_mode == 0) {
           const u32x4 w = wiener_words(uint32_t(site_of(v)), gstep, seed, id);
-          xi_lo = normal_pair(w.x, w.y, R(0));
-          xi_hi = normal_pair(w.z, w.w, R(0));
+          xi_lo = Wiener<R>::term(w.x, w.y, a);
+          xi_hi = Wiener<R>::term(w.z, w.w, a);
         } else {
           const T* nz = noise_tr + int64_t(gstep) * N;
-          xi_lo = valid_of(v) ? nz[site_of(v)] : cmake<T>(R(0), R(0));
-          xi_hi = valid_of(v + H) ? nz[site_of(v + H)] : cmake<T>(R(0), R(0));
+          xi_lo = Wiener<R>::buffer(valid_of(v) ? nz[site_of(v)] : cmake<T>(R(0), R(0)), dt4);
+          xi_hi = Wiener<R>::buffer(valid_of(v + H) ? nz[site_of(v + H)] : cmake<T>(R(0), R(0)), dt4);
         }
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
@@ -678,7 +700,7 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
           T h;
           if constexpr (HOP == 0) h = hop_table(vv);
           else h = ok ? (q ? hop_stencil(p, rh, ch) : hop_stencil(p, rl, cl)) : cmake<T>(R(0), R(0));
-          beta[vv] = local_update(beta[vv], h, r, u, f, dt, dt4, q ? xi_hi : xi_lo);
+          beta[vv] = local_update(beta[vv], h, r, u, f, dt, Wiener<R>::scale(dt4), q ? xi_hi : xi_lo);
           if (!FAST && a.work != nullptr && ok && active) {
             R fd = R(0);
             if (timedep && gstep > 0) {  // Re F = Im(i F); the first step of a run has F(t - dt) = F(t)
@@ -753,7 +775,7 @@ __device__ __forceinline__ void rowrun_body(const StepArgs& a, unsigned char* sm
   const int tpt = half / 4, tpc = CTA / tpt;
   const int tid = threadIdx.x, slot = tid / tpt, t = tid % tpt;
   const bool in_slot = slot < tpc;
-  const float J = a.f_J, dt = a.f_dt, dt4 = a.f_dt4;
+  const float J = a.f_J, dt = a.f_dt;
   const T rsl_s = make_float2(a.f_par[0], a.f_par[1]);
   const T iU_s = make_float2(a.f_par[2], a.f_par[3]);
   const T iF_s = make_float2(a.f_par[4], a.f_par[5]);
@@ -814,14 +836,14 @@ __device__ __forceinline__ void rowrun_body(const StepArgs& a, unsigned char* sm
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const u32x4 w = wiener_words(uint32_t(p0[0] + j), gstep, seed, id);
-        const T xi[2] = {normal_pair(w.x, w.y, 0.0f), normal_pair(w.z, w.w, 0.0f)};
+        const T xi[2] = {Wiener<float>::term(w.x, w.y, a), Wiener<float>::term(w.z, w.w, a)};
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
           const int p = p0[k] + j;
           const T r = g_rsl ? __ldg(g_rsl + p) : rsl_s;
           const T u = g_iU ? __ldg(g_iU + p) : iU_s;
           const T f = g_iF ? __ldg(g_iF + p) : iF_s;
-          v[k][j] = local_update(v[k][j], h[k][j], r, u, f, dt, dt4, xi[k]);
+          v[k][j] = local_update(v[k][j], h[k][j], r, u, f, dt, 1.0f, xi[k]);
         }
       }
       if (a.dbuf) buf ^= 1; else __syncthreads();
@@ -964,12 +986,12 @@ __device__ __forceinline__ void lieb_cell_body(const StepArgs& a, unsigned char*
         const int plo = 3 * t + j, phi = half + plo;
         if (a.noise_mode == 0) {
           const u32x4 w = wiener_words(uint32_t(plo), gstep, seed, id);
-          xi_lo = normal_pair(w.x, w.y, R(0));
-          xi_hi = normal_pair(w.z, w.w, R(0));
+          xi_lo = Wiener<R>::term(w.x, w.y, a);
+          xi_hi = Wiener<R>::term(w.z, w.w, a);
         } else {
           const T* nz = noise_tr + int64_t(gstep) * N;
-          xi_lo = nz[plo];
-          xi_hi = nz[phi];
+          xi_lo = Wiener<R>::buffer(nz[plo], dt4);
+          xi_hi = Wiener<R>::buffer(nz[phi], dt4);
         }
 #pragma unroll
         for (int q = 0; q < 2; ++q) {
@@ -982,7 +1004,7 @@ __device__ __forceinline__ void lieb_cell_body(const StepArgs& a, unsigned char*
             const T f1 = __ldg(reinterpret_cast<const T*>(a.ft_slopes) + int64_t(id_t) * N + p);
             f = cmake<T>(f0.x + dtt * f1.x, f0.y + dtt * f1.y);
           }
-          b[v] = local_update(b[v], h[v], r, u, f, dt, dt4, q ? xi_hi : xi_lo);
+          b[v] = local_update(b[v], h[v], r, u, f, dt, Wiener<R>::scale(dt4), q ? xi_hi : xi_lo);
         }
       }
       if (a.dbuf) buf ^= 1; else __syncthreads();
@@ -1081,12 +1103,12 @@ __device__ __forceinline__ void ell_cluster_body(const StepArgs& a, unsigned cha
         T xi_lo, xi_hi;
         if (a.noise_mode == 0) {
           const u32x4 w = wiener_words(uint32_t(pl), gstep, seed, id);
-          xi_lo = normal_pair(w.x, w.y, R(0));
-          xi_hi = normal_pair(w.z, w.w, R(0));
+          xi_lo = Wiener<R>::term(w.x, w.y, a);
+          xi_hi = Wiener<R>::term(w.z, w.w, a);
         } else {
           const T* nz = noise_tr + int64_t(gstep) * N;
-          xi_lo = nz[pl];
-          xi_hi = ph < N ? nz[ph] : cmake<T>(R(0), R(0));
+          xi_lo = Wiener<R>::buffer(nz[pl], dt4);
+          xi_hi = Wiener<R>::buffer(ph < N ? nz[ph] : cmake<T>(R(0), R(0)), dt4);
         }
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
@@ -1103,7 +1125,8 @@ __device__ __forceinline__ void ell_cluster_body(const StepArgs& a, unsigned cha
           const T ff = g_iF ? __ldg(g_iF + p) : iF_s;
           const int slot = (k ? q : 0) + j;
           const T cur = lds_c((b ? oa1 : oa0) + uint32_t(slot) * TS, T{});
-          sts_c((b ? oa0 : oa1) + uint32_t(slot) * TS, local_update(cur, h, rr, uu, ff, dt, dt4, k ? xi_hi : xi_lo));
+          sts_c((b ? oa0 : oa1) + uint32_t(slot) * TS,
+                local_update(cur, h, rr, uu, ff, dt, Wiener<R>::scale(dt4), k ? xi_hi : xi_lo));
         }
         cl_ += dc; rl += dr; if (cl_ >= ny) { cl_ -= ny; ++rl; }
         ch += dc; rh += dr; if (ch >= ny) { ch -= ny; ++rh; }
@@ -1209,12 +1232,12 @@ __device__ __forceinline__ void ell_cluster_pow2_body(const StepArgs& a, unsigne
         T xi_lo, xi_hi;
         if (FAST || a.noise_mode == 0) {
           const u32x4 w = wiener_words(uint32_t(pl), gstep, seed, id);
-          xi_lo = normal_pair(w.x, w.y, 0.0f);
-          xi_hi = normal_pair(w.z, w.w, 0.0f);
+          xi_lo = Wiener<float>::term(w.x, w.y, a);
+          xi_hi = Wiener<float>::term(w.z, w.w, a);
         } else {
           const T* nz = noise_tr + int64_t(gstep) * N;
-          xi_lo = nz[pl];
-          xi_hi = nz[pl + half];
+          xi_lo = Wiener<float>::buffer(nz[pl], dt4);
+          xi_hi = Wiener<float>::buffer(nz[pl + half], dt4);
         }
 #pragma unroll
         for (int k = 0; k < 2; ++k) {
@@ -1233,7 +1256,7 @@ __device__ __forceinline__ void ell_cluster_pow2_body(const StepArgs& a, unsigne
           const T uu = !FAST && g_iU ? __ldg(g_iU + p) : iU_s;
           const T ff = !FAST && g_iF ? __ldg(g_iF + p) : iF_s;
           const T v = lds_c(cur + sl * TS, T{});
-          sts_c(nxt + sl * TS, local_update(v, h, rr, uu, ff, dt, dt4, k ? xi_hi : xi_lo));
+          sts_c(nxt + sl * TS, local_update(v, h, rr, uu, ff, dt, 1.0f, k ? xi_hi : xi_lo));
         }
       }
       b ^= 1;

@@ -45,18 +45,22 @@ def test_device_normals_are_the_philox_stream(built_lib, oracle):
             assert d.max() < tol, (prec, k, d.max())
 
 
-def test_headline_kernel_matches_oracle(built_lib, oracle):
+@pytest.mark.parametrize("L,disorder", [(64, True), (64, False), (32, True)])
+def test_headline_kernel_matches_oracle(built_lib, oracle, L, disorder):
     """The exact kernel of the headline workload (64x64, per-site omega, FP32
-    Philox, the fast instantiation) for 500 steps (two 250-step frames) from
+    Philox: the fast instantiation of the register-FFT kernel), with scalar
+    omega, and on 32x32, for 500 steps (two 250-step frames) from
     device-drawn initial fields: every frame and the final field of each
     trajectory equal the FP64 oracle's (TWMCBaseSolver.cpp:232-266) fed the
     same Wiener normals (twmc_debug_wiener) and the drawn omega realisation,
     within 1e-5 relative."""
-    nx = ny = 64
+    nx = ny = L
     n = nx * ny
     ntraj, fs, nfr = 3, 250, 2
     steps = fs * nfr
-    sysd = _system(nx, ny, twmc.PREC_F32, fs)
+    sysd = twmc.System(nx=nx, ny=ny, J=J, gamma=GAMMA, dt=DT, frame_steps=fs,
+                       omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2) if disorder else -0.5, U=U, F=F,
+                       beta_init=0.0, beta_init_sigma=0.5, precision=twmc.PREC_F32)
     tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=steps * DT, seed0=901, id0=40)
     res = sysd.run(tasks, frames=True, realizations=True)
     kernel = sysd.kernel_name
@@ -65,8 +69,9 @@ def test_headline_kernel_matches_oracle(built_lib, oracle):
     assert (res["status"] == 0).all()
     for k in range(ntraj):
         xi = twmc.debug_wiener(twmc.PREC_F32, 901 + k, 40 + k, steps, n)
-        ref = oracle.base_run(nx, ny, J, GAMMA, DT, 0.0, steps * DT, fs, nfr + 1, True, res["omega_realization"][k],
-                              U, F, res["frames"][k, 0], xi=xi)
+        om = res["omega_realization"][k] if disorder else -0.5
+        ref = oracle.base_run(nx, ny, J, GAMMA, DT, 0.0, steps * DT, fs, nfr + 1, True, om, U, F,
+                              res["frames"][k, 0], xi=xi)
         assert ref["steps"] == steps
         assert res["frames_written"][k] == ref["frames_written"] == nfr + 1
         e = rel_err(res["frames"][k], ref["frames"])

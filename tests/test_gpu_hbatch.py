@@ -58,10 +58,10 @@ def test_hbatch_matches_single_point_runs(built_lib):
     for i, p in enumerate(POINTS):
         f, m, kname = single(p, 3)
         plan = hb.plan(i)
-        assert ("hbatch" in plan) == kname.startswith("square_fft_kernel"), (plan, kname)
+        assert ("hbatch" in plan) == kname.startswith("square_"), (plan, kname)
         st = hb.state(i)
         hm = hb.moments(i)
-        if kname.startswith("square_fft_kernel"):
+        if kname.startswith("square_"):  # FFT kernels
             e = np.abs(st - f).max() / np.abs(f).max()
             assert e < 1e-5, f"point {i} ({plan}): rel diff {e:.2e}"
             for c in range(3):  # |a|^2, |a|^4, |a_k|^2 block sums, each relative to its largest
