@@ -114,6 +114,31 @@ def _profile_figure(key, profile="square_fft_kernel_64x64.md"):
     return float(m.group(1)) if m else None
 
 
+def _profile_source(profile):
+    """Where a profile figure came from: the summary file and its `captured:`
+    line (date and commit of the capture), so that stale figures show."""
+    import re
+    try:
+        txt = open(os.path.join(ROOT, "profiles", profile)).read()
+    except OSError:
+        return None
+    m = re.search(r"captured:\s*(.+)", txt)
+    return {"file": f"profiles/{profile}", "captured": m.group(1).strip() if m else "unrecorded"}
+
+
+def issue_fraction(rate, profile, sm_mhz, torch):
+    """Warp-instruction issue rate of a kernel: site-updates/s x ncu's thread
+    instructions per site-update / 32, against one instruction per cycle per
+    scheduler (SMs x 4 x the median SM clock of the run)."""
+    ipsu = _profile_figure("inst_per_site_update", profile)
+    if not ipsu or not sm_mhz:
+        return None
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    ach = rate * ipsu / 32.0
+    return {"inst_per_site_update": ipsu, "frac": ach / (sms * 4 * sm_mhz * 1e6),
+            "profile": _profile_source(profile)}
+
+
 def ncu_traffic():
     """DRAM bytes per step-kernel launch at the full workload (ncu, scaled from the small capture)."""
     return _profile_figure("dram_bytes_per_launch_full_size")
@@ -138,42 +163,13 @@ def make_system(twmc, hop=None, precision=None):
                        hop=twmc.HOP_FFT if hop is None else hop, n_moment_blocks=32)
 
 
-def measure_other_paths(twmc, torch, sm_mhz=None):
-    """Throughput of the other configurations, one timed unit each: the
-    headline workload on the real-space stencil kernel (the same hopping
-    operator applied without the FFT), the 256-point heterogeneous batch
-    (chains of 32..1024 sites and 16..128 square lattices, 512..4096
-    trajectories per point, one frame of 250 steps in one graph launch), and
-    the 1-D Lieb lattice (256 cells, U disorder, F(t) ramp, 8192 trajectories,
-    1000 steps through twmc_run)."""
+def batch_points(seed=3):
+    """The heterogeneous-batch workload: 256 parameter points, each a chain of
+    32..1024 sites or an L x L lattice (L = 16..128), U ~ U[0.05, 0.5],
+    detuning ~ U[-2, 2], F ~ U[0, 3], J = gamma = 1, 512..4096 trajectories
+    (uniform in log), dt = 0.002, frames of 250 steps."""
     import numpy as np
-    out = {}
-    sysd = make_system(twmc, hop=twmc.HOP_STENCIL)
-    sysd.batch_init(sysd.make_tasks(NTRAJ, t_start=0.0, t_end=T_END, seed0=5, id0=1))
-    sysd.advance(FRAME_STEPS)
-    sysd.sync()
-    ext = torch.cuda.ExternalStream(sysd.stream)
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(ext)
-    for _ in range(2):
-        sysd.advance(FRAME_STEPS)
-    e1.record(ext)
-    sysd.sync()
-    ms = e0.elapsed_time(e1) / 2
-    out["headline_real_space"] = {"value": FRAME_STEPS * NTRAJ * NX * NY / (ms / 1e3), "unit": METRIC,
-                                  "kernel": sysd.kernel_name, "ms_per_frame": ms}
-    kname = out["headline_real_space"]["kernel"]
-    prof = "rowrun_kernel_64x64.md" if kname == "rowrun_kernel" else "ell_kernel_64x64_stencil.md"
-    ipsu = _profile_figure("inst_per_site_update", prof)
-    if ipsu and sm_mhz:
-        sms = torch.cuda.get_device_properties(0).multi_processor_count
-        ach = out["headline_real_space"]["value"] * ipsu / 32.0
-        out["headline_real_space"]["issue"] = {
-            "inst_per_site_update": ipsu, "frac": ach / (sms * 4 * sm_mhz * 1e6),
-            "source": f"ncu instruction count (profiles/{prof}) x measured rate; "
-                      "peak = SMs x 4 schedulers x median SM clock of the headline run"}
-    sysd.close()
-    rng = np.random.default_rng(3)
+    rng = np.random.default_rng(seed)
     kinds = [(1, n) for n in (32, 64, 128, 256, 512, 1024)] + [(l, l) for l in (16, 32, 64, 128)]
     pts = []
     for _ in range(256):
@@ -181,21 +177,81 @@ def measure_other_paths(twmc, torch, sm_mhz=None):
         pts.append(dict(nx=nx, ny=ny, U=rng.uniform(0.05, 0.5), omega=rng.uniform(-2, 2), F=rng.uniform(0, 3),
                         dt=DT, n_traj=int(np.exp(rng.uniform(np.log(512), np.log(4096)))),
                         seed0=int(rng.integers(1, 2 ** 31)), id0=1))
+    return pts
+
+
+def measure_batch(twmc, torch, sm_mhz=None, t_end=60.0):
+    """The 256-point heterogeneous batch to its full t_end (120 frames of 250
+    steps), autotuned step variants, every (point, trajectory group) a work
+    item of the persistent queue kernels; device time of the whole run."""
+    from collections import Counter
+    pts = batch_points()
     sites = sum(p["nx"] * p["ny"] * p["n_traj"] for p in pts)
+    frames = int(round(t_end / (DT * FRAME_STEPS)))
     hb = twmc.HBatch(pts, FRAME_STEPS, tune=True)
-    hb.run(1)
+    plans = [hb.plan(i) for i in range(len(pts))]
+    hb.run(1)  # untimed first frame
     hb.sync()
-    hb.run(1)
+    hb.run(frames)
     ms = hb.sync()
-    out["heterogeneous_batch"] = {"value": FRAME_STEPS * sites / (ms / 1e3), "unit": METRIC, "points": len(pts),
-                                  "ms_per_frame": ms, "autotuned": True}
+    bm = hb.block_means()
+    import numpy as np
+    finite = bool(all(np.isfinite(b).all() for b in bm))
     hb.close()
+    rate = frames * FRAME_STEPS * sites / (ms / 1e3)
+    out = {"value": rate, "unit": METRIC, "points": len(pts), "t_end": t_end, "frames": frames,
+           "device_s": ms / 1e3, "trajectories_per_s": sum(p["n_traj"] for p in pts) * (frames / (frames + 1)) /
+           (ms / 1e3), "finite": finite, "autotuned": True,
+           "kernels": dict(Counter(p.split("<")[0] for p in plans)),
+           "variants": dict(sorted(Counter(p.split("<")[1].rstrip(">") for p in plans).items())),
+           "timing": "CUDA events around the graph replays of frames 2..121 (t = 0.5..60.5)"}
+    iss = issue_fraction(rate, "hbatch_256_points.md", sm_mhz, torch)
+    if iss:
+        out["issue"] = iss
+    return out
+
+
+def measure_other_paths(twmc, torch, sm_mhz=None):
+    """Throughput of the other configurations, device-timed: the headline
+    workload on the real-space stencil kernel (the same hopping operator
+    applied without the FFT), the 256-point heterogeneous batch to t = 60,
+    the 1-D Lieb lattice (256 cells, U disorder, F(t) ramp, 8192
+    trajectories) and the 128 x 128 lattice on the 2-CTA cluster kernel
+    (4096 trajectories), each with its issue-rate fraction; the Lieb workload
+    also through twmc_run (host wall clock, initial draws included)."""
     from pincosimulator_gb300 import workloads
+    out = {}
+    sysd = make_system(twmc, hop=twmc.HOP_STENCIL)
+    s = workloads.time_batch(sysd, NTRAJ, 2)
+    r = FRAME_STEPS * NTRAJ * NX * NY * 2 / s
+    out["headline_real_space"] = {"value": r, "unit": METRIC, "kernel": sysd.kernel_name, "ms_per_frame": s * 500}
+    prof = "rowrun_kernel_64x64.md" if sysd.kernel_name == "rowrun_kernel" else "ell_kernel_64x64_stencil.md"
+    out["headline_real_space"]["issue"] = issue_fraction(r, prof, sm_mhz, torch)
+    sysd.close()
+    out["heterogeneous_batch"] = measure_batch(twmc, torch, sm_mhz)
     sysd = workloads.lieb()
-    el, _ = workloads.time_run(sysd, 8192, 4)
-    out["lieb"] = {"value": sysd.n_sites * 8192 * 1000 / el, "unit": METRIC, "kernel": sysd.kernel_name,
-                   "timing": "host wall clock around one twmc_run call of 1000 steps (initial draws and frame "
-                             "bookkeeping included)"}
+    tasks = sysd.make_tasks(8192, t_end=4 * FRAME_STEPS * DT, store_initial=False)
+    sysd.run(tasks, frames=False, final=False)  # untimed; the F(t) table runs through twmc_run
+    sysd.sync()
+    t0 = time.perf_counter()
+    sysd.run(tasks, frames=False, final=False)
+    el = time.perf_counter() - t0
+    kms = sysd.sync()  # CUDA-event time of the step launches of the timed call
+    r = sysd.n_sites * 8192 * 1000 / (kms / 1e3)
+    out["lieb"] = {"value": r, "unit": METRIC, "kernel": sysd.kernel_name, "kernel_ms_per_1000_steps": kms,
+                   "workload": "1-D Lieb 256 cells x 3, PBC, U = 0.27 + 0.06 U[0,1), F(t) ramp on B sites, "
+                               "8192 trajectories, 1000 steps (CUDA events around the step launches)",
+                   "issue": issue_fraction(r, "lieb_cell_kernel_lieb768.md", sm_mhz, torch),
+                   "twmc_run": {"value": sysd.n_sites * 8192 * 1000 / el, "unit": METRIC,
+                                "timing": "host wall clock around the twmc_run call (initial draws and frame "
+                                          "bookkeeping included)"}}
+    sysd.close()
+    sysd = workloads.square(128, 128, hop=twmc.HOP_STENCIL)
+    s = workloads.time_batch(sysd, 4096, 1)
+    r = 128 * 128 * 4096 * FRAME_STEPS / s
+    out["square128"] = {"value": r, "unit": METRIC, "kernel": sysd.kernel_name, "ms_per_frame": s * 1e3,
+                        "workload": "128x128 PBC, the headline parameters, 4096 trajectories, one 250-step frame",
+                        "issue": issue_fraction(r, "ell_cluster_pow2_kernel_128x128.md", sm_mhz, torch)}
     sysd.close()
     return out
 
@@ -254,62 +310,145 @@ def measure_observable_error(twmc, ntraj=256, t_end=T_END):
                      "n_site_avg.max_rel_diff = max over frames of |nbar32 - nbar64| / nbar64"}
 
 
-def cpu_baseline(target_s=12.0, threads=None):
-    """Oracle port (FP64 restatement, radix-2 FFT, not FFTW) on the host cores:
-    a bounded sample of the same workload (trajectories x 250 steps of 64 x 64)."""
+def _cpu_cores():
+    """Host CPU description for the baseline record."""
+    model = ""
+    try:
+        for line in open("/proc/cpuinfo"):
+            k = line.split(":")[0].strip().lower()
+            if k in ("model name", "cpu model", "uarch") and not model:
+                model = line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return os.cpu_count() or 1, model
+
+
+def cpu_run(ntraj, steps, threads, build, noise):
+    """Wall time of ntraj trajectories x `steps` steps of the 64 x 64
+    workload through the oracle's threaded batch (one trajectory per task on
+    `threads` workers, as the reference's ThreadedTaskProcessor)."""
     import numpy as np
     from oracle import loader as orc
 
-    lib = orc.load(fast=True)
-    threads = threads or os.cpu_count() or 1
+    lib = orc.load(fast=build)
     n = NX * NY
     rng = np.random.default_rng(0)
     omega = np.ascontiguousarray(-0.5 + 0.2 * rng.normal(size=n) + 0j)
     U = np.full(n, 0.2 + 0j)
     F = np.full(n, 2.0 + 0j)
     b0 = np.ascontiguousarray(0.5 * (rng.normal(size=n) + 1j * rng.normal(size=n)))
+    t0 = time.perf_counter()
+    done = lib.orc_base_run_batch(NX, NY, 1.0, 1.0, DT, 0.0, (steps - 0.5) * DT, steps, 2, omega.ctypes.data,
+                                  U.ctypes.data, F.ctypes.data, b0.ctypes.data, ntraj, 1, threads, None,
+                                  orc.NOISE[noise])
+    return done, time.perf_counter() - t0
 
-    def run(ntraj, steps):
-        t0 = time.perf_counter()
-        done = lib.orc_base_run_batch(NX, NY, 1.0, 1.0, DT, 0.0, (steps - 0.5) * DT, steps, 2, omega.ctypes.data,
-                                      U.ctypes.data, F.ctypes.data, b0.ctypes.data, ntraj, 1, threads, None)
-        return done, time.perf_counter() - t0
 
+def cpu_baseline(target_s=12.0, threads=None):
+    """The CPU restatement of the reference's loop (FP64, the oracle's FFT,
+    not FFTW) on all host threads, timed on a bounded sample of the same
+    workload (trajectories x 25 steps of 64 x 64): the headline figure uses
+    the reference's own release flags (-Ofast -march=native) and noise
+    generator (std::mt19937 + std::normal_distribution, as randCMat); the
+    -O3 build with the GPU solver's Philox stream is reported beside it."""
+    from oracle import build_oracle
+
+    cores, model = _cpu_cores()
+    threads = threads or cores
     steps = 25
-    _, t1 = run(threads, steps)  # calibration: one trajectory per thread
-    per_round = max(t1, 1e-3)
-    rounds = max(1, int(target_s / per_round))
-    ntraj = threads * rounds
-    done, el = run(ntraj, steps)
-    su = float(done) * steps * n
-    return {"value": su / el, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"{done} trajectories x {steps} steps of 64x64 (FP64 oracle restatement, radix-2 FFT, not "
-                      f"FFTW), {el:.1f} s"}
+    out = {}
+    for key, build, noise, share in (("ref_flags_mt19937", "ref_flags", "mt19937", 0.7),
+                                     ("O3_philox", True, "philox64", 0.3)):
+        _, t1 = cpu_run(threads, steps, threads, build, noise)  # calibration: one trajectory per thread
+        rounds = max(1, int(share * target_s / max(t1, 1e-3)))
+        done, el = cpu_run(threads * rounds, steps, threads, build, noise)
+        out[key] = {"value": float(done) * steps * NX * NY / el, "seconds": round(el, 2),
+                    "sample": f"{done} trajectories x {steps} steps", "flags": build_oracle.build_flags(build),
+                    "noise": noise}
+    head = out["ref_flags_mt19937"]
+    return {"value": head["value"], "unit": METRIC, "cores": threads, "kind": "port", "cpu": model,
+            "sample": f"{head['sample']} of 64x64 in {head['seconds']} s; FP64 restatement of "
+                      f"TWMCBaseSolver's loop with the reference's flags ({head['flags']}) and noise generator "
+                      "(mt19937 + normal_distribution); batched radix-2 FFT, not FFTW",
+            "variants": out}
 
 
 def run_reference(args):
+    """The reference arm: the CPU restatement of the reference's loop with the
+    reference's flags and noise generator on all host threads, each step a
+    bounded sample of the headline workload (trajectories x 25 steps of
+    64 x 64) timed on its own; value = the median sample rate."""
     rank, world, _ = env_rank()
     if rank != 0:
         return 0
-    steps = args.steps
-    vals = []
-    for i in range(args.warmup + steps):
-        cb = cpu_baseline(target_s=max(2.0, 60.0 / max(1, args.warmup + steps)))
+    from oracle import build_oracle
+
+    build_oracle.build()
+    cores, model = _cpu_cores()
+    steps = 25
+    _, t1 = cpu_run(cores, steps, cores, "ref_flags", "mt19937")
+    per_step_s = max(2.0, 45.0 / max(1, args.warmup + args.steps))
+    rounds = max(1, int(per_step_s / max(t1, 1e-3)))
+    samples = []
+    for i in range(args.warmup + args.steps):
+        done, el = cpu_run(cores * rounds, steps, cores, "ref_flags", "mt19937")
         if i >= args.warmup:
-            vals.append(cb)
-    v = statistics.median(c["value"] for c in vals)
-    ms = 1e3 * (NTRAJ * NX * NY * FRAME_STEPS) / v
+            samples.append((done, el))
+    rates = [d * steps * NX * NY / e for d, e in samples]
+    v = statistics.median(rates)
+    sample = f"{samples[0][0]} trajectories x {steps} steps of 64x64 per step"
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
-            "steps": steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * statistics.median(e for _, e in samples), "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic", "config": CONFIG,
-            "cpu_baseline": {"value": v, "unit": METRIC, "cores": vals[0]["cores"], "kind": "port",
-                             "sample": vals[0]["sample"]},
+            "sample_site_updates_per_step": samples[0][0] * steps * NX * NY,
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": cores, "kind": "port", "cpu": model,
+                             "sample": sample, "flags": build_oracle.build_flags("ref_flags"),
+                             "noise": "mt19937 + normal_distribution (randCMat)"},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
             "note": "the reference cannot be built here (FFTW3/Eigen3/cpptoml/CLI11/easylogging++ absent); the "
-                    "arm runs the oracle's FP64 restatement of TWMCBaseSolver's loop on all host threads; "
-                    "ms_per_step extrapolates the per-site rate to one full bench step"}
+                    "arm runs the oracle's FP64 restatement of TWMCBaseSolver's loop with the reference's release "
+                    "flags and noise generator, one trajectory per task on all host threads; each bench step is "
+                    "one timed sample (ms_per_step is that sample's wall time, not the full 16384-trajectory "
+                    "frame)"}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def measure_e2e(twmc, torch, args, frames=True):
+    """Site-updates/s through twmc_run with host result buffers: one call
+    runs e2e_steps frames of all 16384 trajectories (initial draws and
+    disorder on the GPU inside the call) and returns, into pinned host arrays
+    allocated once and reused as a production caller would, every saved frame
+    (complex128, the reference's traj dataset) when `frames`, the final field
+    and the FP64 moment blocks of every frame. Mean of two calls after one
+    warm-up call."""
+    sysd = make_system(twmc, twmc.HOP_STENCIL if args.hop == "stencil" else None)
+    n_fr = args.e2e_steps
+    tasks = sysd.make_tasks(NTRAJ, t_start=0.0, t_end=n_fr * FRAME_STEPS * DT, seed0=7, store_initial=False)
+    bufs = {"final": torch.empty((NTRAJ, NX * NY), dtype=torch.complex128, pin_memory=True).numpy(),
+            "moments": torch.empty((n_fr, 32, NX * NY, 3), dtype=torch.float64, pin_memory=True).numpy()}
+    if frames:
+        bufs["frames"] = torch.empty((NTRAJ, n_fr, NX * NY), dtype=torch.complex128, pin_memory=True).numpy()
+    sysd.run(tasks, frames=frames, final=True, moments=True, buffers=bufs)
+    calls = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        res = sysd.run(tasks, frames=frames, final=True, moments=True, buffers=bufs)
+        calls.append(time.perf_counter() - t0)
+    el = sum(calls) / len(calls)
+    sysd.close()
+    h2d = (NTRAJ * (8 + 8) + 5 * 2 * NX * NY * 16) / n_fr  # seeds, ids, base / amplitude matrices
+    d2h = (sum(b.nbytes for b in bufs.values()) + NTRAJ * (8 + 8 + 4)) / n_fr
+    assert res["frames_written"].min() == n_fr
+    out = {"value": n_fr * FRAME_STEPS * NTRAJ * NX * NY / el, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
+           "d2h_bytes_per_step": int(d2h), "calls_ms": [round(c * 1e3, 2) for c in calls],
+           "api": "twmc_run into pinned host result arrays reused across calls: " +
+                  ("every frame of every trajectory (complex128, widened on the GPU), " if frames else "") +
+                  "the final field, FP64 moment blocks of every frame; initial draws and disorder on the GPU "
+                  "inside the call; mean of 2 calls after 1 warm-up"}
+    del res, bufs
+    return out
 
 
 def main():
@@ -381,11 +520,26 @@ def main():
     launches = sysd.launch_count - launches0
     clocks = clock_sampler_stop(proc, fh, clk_path, int(os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0])
                                 if world > 1 else 0)
-    field, _ = sysd.download(field=True, moments=False)
+    field, mom = sysd.download(field=True, moments=True)
     import numpy as np
 
     finite = bool(np.isfinite(field).all())
     del field
+    # replicas: every rank's FP64 moment blocks of its own trajectories,
+    # gathered in rank order on the host (gloo) -- the only exchange of the
+    # path; the merged blocks are those of one run of all ranks' trajectories
+    from pincosimulator_gb300 import observables as obmod, replicas
+
+    if dist:
+        gloo = dist.new_group(backend="gloo")
+        merged = replicas.gather_blocks(mom, group=gloo)
+    else:
+        merged = mom
+    ens = obmod.observables(merged, ntraj * world)
+    ensemble = {"ranks": world, "trajectories": ntraj * world, "blocks": int(merged.shape[0]),
+                "n_site_avg": float(np.mean(ens["n"])), "g2_site_avg": float(np.nanmean(ens["g2"])),
+                "merge": "moment blocks gathered in rank order (replicas.gather_blocks over gloo)" if dist else
+                         "single rank"}
     info_kernel = sysd.kernel_name
     sysd.close()
     su_rank = float(args.steps) * FRAME_STEPS * ntraj * NX * NY
@@ -397,34 +551,14 @@ def main():
     value = su_rank * world / (t_max / 1e3)
     # roofline of the dominant kernel (the step kernel; the moments kernel is < 1%)
     achieved = su_rank * FLOPS_PER_SITE_UPDATE / (kernel_ms / 1e3) / 1e12
-    # end to end through the C ABI with host buffers (twmc_run)
+    # end to end through the C ABI with host buffers (twmc_run): every saved
+    # frame of every trajectory (the reference's "traj" dataset,
+    # TWMCBaseSolver.cpp:257-277) plus the moment blocks; the same call
+    # without frames beside it
     e2e = None
     if not args.no_e2e:
-        sysd = make_system(twmc, twmc.HOP_STENCIL if args.hop == "stencil" else None)
-        tasks = sysd.make_tasks(NTRAJ, t_start=0.0, t_end=args.e2e_steps * FRAME_STEPS * DT, seed0=7,
-                                store_initial=False)
-        # result buffers in pinned host memory, allocated once and reused by
-        # every call as a production caller would; one untimed warm-up call
-        bufs = {"final": torch.empty((NTRAJ, NX * NY), dtype=torch.complex128, pin_memory=True).numpy(),
-                "moments": torch.empty((args.e2e_steps, 32, NX * NY, 3), dtype=torch.float64,
-                                       pin_memory=True).numpy()}
-        sysd.run(tasks, frames=False, final=True, moments=True, buffers=bufs)
-        reps = 2
-        calls = []
-        for _ in range(reps):
-            t0 = time.perf_counter()
-            res = sysd.run(tasks, frames=False, final=True, moments=True, buffers=bufs)
-            calls.append(time.perf_counter() - t0)
-        el = sum(calls) / reps
-        sysd.close()
-        n_fr = args.e2e_steps
-        h2d = (NTRAJ * (8 + 8) + 5 * 2 * NX * NY * 16) / n_fr
-        d2h = (res["final"].size * 8 + n_fr * 32 * NX * NY * 3 * 8 + NTRAJ * (8 + 8 + 4)) / n_fr
-        e2e = {"value": n_fr * FRAME_STEPS * NTRAJ * NX * NY / el, "unit": METRIC, "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h), "calls_ms": [round(c * 1e3, 2) for c in calls], "api": "twmc_run (pinned host result buffers reused across calls: "
-               "final field widened to complex128 on the GPU, FP64 moment blocks every frame; initial draws and "
-               "disorder on the GPU inside the call; mean of 2 calls after 1 warm-up)"}
-        del res
+        e2e = measure_e2e(twmc, torch, args, frames=True)
+        e2e["no_frames"] = measure_e2e(twmc, torch, args, frames=False)
     if rank != 0:
         if dist:
             dist.destroy_process_group()
@@ -432,15 +566,8 @@ def main():
     peaks = measured_peaks()
     # instruction-issue roofline: ncu's instructions per site-update x the
     # measured rate, against one warp instruction per cycle per scheduler
-    ipsu = _profile_figure("inst_per_site_update")
-    issue = None
-    if ipsu and clocks and clocks.get("sm_mhz"):
-        sms = torch.cuda.get_device_properties(0).multi_processor_count
-        ach = su_rank / (kernel_ms / 1e3) * ipsu / 32.0
-        pk = sms * 4 * clocks["sm_mhz"] * 1e6
-        issue = {"inst_per_site_update": ipsu, "achieved_warp_inst_per_s": ach, "peak_warp_inst_per_s": pk,
-                 "frac": ach / pk, "source": "ncu instruction count (profiles/square_fft_kernel_64x64.md) x "
-                 "measured rate; peak = SMs x 4 schedulers x median SM clock"}
+    issue = issue_fraction(su_rank / (kernel_ms / 1e3), "square_fft_kernel_64x64.md",
+                           clocks.get("sm_mhz") if clocks else None, torch)
     cpu = None if (args.no_cpu_baseline or world > 1) else cpu_baseline()
     warm = None if (args.no_warm or world > 1) else measure_warm_start()
     f64 = None
@@ -461,6 +588,7 @@ def main():
         "config": dict(CONFIG, hop=args.hop, kernel=info_kernel, trajectories=ntraj),
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                      "frac": achieved / fp32_peak if fp32_peak else None, "traffic": ncu_traffic(),
+                     "traffic_profile": _profile_source("square_fft_kernel_64x64.md"),
                      "peak_source": "measured in this run: FP32 FMA chain over all SMs (twmc_measure_fp32_peak)",
                      "flops_per_site_update": FLOPS_PER_SITE_UPDATE,
                      "hbm": {"achieved_gbs": su_rank * BYTES_PER_SITE_UPDATE_HBM / (kernel_ms / 1e3) / 1e9,
@@ -468,7 +596,7 @@ def main():
         "issue": issue, "e2e": e2e, "gpu_launches": launches, "cpu_baseline": cpu, "clocks": clocks,
         "trajectories_per_s": value / (NX * NY * (T_END / DT)), "finite": finite,
         "kernel_ms": kernel_ms, "time_to_steady_state": warm, "fp64_mode": f64, "observable_error": obs_err,
-        "other_paths": other,
+        "other_paths": other, "ensemble": ensemble,
     }
     print(json.dumps(line), flush=True)
     if dist:

@@ -234,16 +234,30 @@ typedef struct twmc_point_desc {
 
 typedef struct twmc_hbatch twmc_hbatch;
 
-/* Builds a batch of n points advanced together frame by frame: every point's
- * trajectories of a shape with a register-FFT plan that fits 256 threads
- * (chains of 32..1024 sites, 16x16, 32x32, 64x64 lattices) are served by one
- * persistent launch with an atomic work queue; other shapes run the
- * real-space kernel concurrently. One frame (frame_steps steps of every
- * point, FP64 moment blocks, counters) is captured into a CUDA graph. tune:
- * 1 = per shape, time the FFT path against the real-space path once and keep
- * the faster (cached in $TWMC_TUNE_CACHE or ~/.cache/twmc_tune.json). */
+/* Builds a batch of n points advanced together frame by frame. Every point
+ * takes one step variant -- "fft" (register FFT: chains of 32..1024 sites,
+ * 16x16, 32x32, 64x64), "ell2" / "ell4" / "ell8" (real-space stencil with 2,
+ * 4, 8 sites per thread, 256-thread CTAs, up to 512 / 1024 / 2048 sites),
+ * "rowrun" (runs of four sites along a row, 512-thread CTAs, ny a multiple
+ * of 4, up to 4096 sites), "ell8w" (8 sites per thread, 512-thread CTAs, up
+ * to 4096 sites), "cluster_pow2" / "cluster" (2-CTA clusters, 4097..16384
+ * sites; the power-of-two form for N = 2^k, ny a power of two <= N/4) --
+ * and every (point, trajectory group) is a work item of a persistent
+ * work-queue kernel for its CTA geometry, taken from an atomic counter,
+ * longest items first. One frame (frame_steps steps of every point, FP64
+ * moment blocks, counters) is captured into a CUDA graph. tune: 0 = the
+ * default variant per shape (FFT where a plan exists, else row runs on
+ * 4096-site lattices, the fullest real-space stencil, or the cluster form);
+ * 1 = per shape, time every variant the shape admits once on a trial batch
+ * and keep the fastest (cached in $TWMC_TUNE_CACHE or
+ * ~/.cache/twmc_tune.json). */
 TWMC_API int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_steps, int32_t tune,
                                 twmc_hbatch** out);
+/* The same with the step variant of every point given by name (variants[i],
+ * one of the names above); a variant the point's lattice does not admit
+ * returns TWMC_ERR_INVALID. */
+TWMC_API int twmc_hbatch_create_variants(const twmc_point_desc* points, size_t n, int64_t frame_steps,
+                                         const char* const* variants, twmc_hbatch** out);
 /* Replays the frame graph n_frames times (asynchronous). */
 TWMC_API int twmc_hbatch_run(twmc_hbatch* b, int64_t n_frames);
 /* Waits for the batch; *ms = device time of the last twmc_hbatch_run. */

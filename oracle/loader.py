@@ -37,7 +37,7 @@ def _setup(lib):
                                  C.c_void_p, C.c_int]
     lib.orc_base_run_batch.argtypes = [C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double,
                                        C.c_double, C.c_int64, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
-                                       C.c_void_p, C.c_int64, C.c_uint32, C.c_int, C.c_void_p]
+                                       C.c_void_p, C.c_int64, C.c_uint32, C.c_int, C.c_void_p, C.c_int]
     lib.orc_base_run_batch.restype = C.c_int64
     return lib
 
@@ -81,7 +81,7 @@ def frame_grid(t_start, t_end, timestep, frames_freq=0.0, frames_period=0.0, n_f
             "n_frames": int(out[4])}
 
 
-NOISE = {"buffer": 0, "philox64": 1, "philox32": 2}
+NOISE = {"buffer": 0, "philox64": 1, "philox32": 2, "mt19937": 3}
 
 
 def base_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, store_initial, omega, U, F, beta0,

@@ -38,6 +38,7 @@
 #include <cstdint>
 #include <cstring>
 #include <algorithm>
+#include <random>
 #include <atomic>
 #include <limits>
 #include <thread>
@@ -186,7 +187,64 @@ void fft1d_inplace(cd* x, int64_t n, int64_t stride, int sign, std::vector<cd>& 
   }
 }
 
+// Radix-2 DIT over the row index of a row-major n0 x n1 array (n0 a power
+// of two) for all n1 columns at once: every butterfly runs over the
+// contiguous columns, so the inner loops vectorise. Per column this is
+// exactly fft1d_inplace's arithmetic (same bit reversal, same twiddles in the
+// same order), so the results are bit for bit those of the column loop.
+void fft_rows_batched(cd* x, int64_t n0, int64_t n1, int sign) {
+  for (int64_t i = 1, j = 0; i < n0; ++i) {
+    int64_t bit = n0 >> 1;
+    for (; j & bit; bit >>= 1) j ^= bit;
+    j ^= bit;
+    if (i < j) std::swap_ranges(x + i * n1, x + (i + 1) * n1, x + j * n1);
+  }
+  thread_local std::vector<cd> tw;
+  thread_local int64_t tw_n = 0;
+  thread_local int tw_sign = 0;
+  if (tw_n != n0 || tw_sign != sign) {
+    tw.clear();
+    for (int64_t len = 2; len <= n0; len <<= 1)
+      for (int64_t k = 0; k < len / 2; ++k) {
+        const double ang = sign * 2.0 * M_PI * double(k) / double(len);
+        tw.emplace_back(std::cos(ang), std::sin(ang));
+      }
+    tw_n = n0;
+    tw_sign = sign;
+  }
+  size_t off = 0;
+  for (int64_t len = 2; len <= n0; len <<= 1, off += size_t(len / 4)) {
+    const int64_t h = len / 2;
+    for (int64_t i = 0; i < n0; i += len)
+      for (int64_t k = 0; k < h; ++k) {
+        const cd w = tw[off + size_t(k)];
+        cd* __restrict__ u = x + (i + k) * n1;
+        cd* __restrict__ v = x + (i + k + h) * n1;
+        for (int64_t c = 0; c < n1; ++c) {
+          const cd t = v[c] * w;
+          v[c] = u[c] - t;
+          u[c] = u[c] + t;
+        }
+      }
+  }
+}
+
+void transpose(const cd* in, cd* out, int64_t n0, int64_t n1) {
+  for (int64_t r = 0; r < n0; ++r)
+    for (int64_t c = 0; c < n1; ++c) out[c * n0 + r] = in[r * n1 + c];
+}
+
 void fft2d(cd* x, int64_t n0, int64_t n1, int sign) {
+  const bool pow2 = n0 > 1 && n1 > 1 && (n0 & (n0 - 1)) == 0 && (n1 & (n1 - 1)) == 0;
+  if (pow2) {  // rows (along the column index) through a transpose, then columns
+    thread_local std::vector<cd> t;
+    t.resize(size_t(n0 * n1));
+    transpose(x, t.data(), n0, n1);
+    fft_rows_batched(t.data(), n1, n0, sign);
+    transpose(t.data(), x, n1, n0);
+    fft_rows_batched(x, n0, n1, sign);
+    return;
+  }
   std::vector<cd> tmp;
   for (int64_t r = 0; r < n0; ++r) fft1d_inplace(x + r * n1, n1, 1, sign, tmp);
   for (int64_t c = 0; c < n1; ++c) fft1d_inplace(x + c, n0, n1, sign, tmp);
@@ -346,6 +404,7 @@ static int square_run(int64_t nx, int64_t ny, double J, double gamma, double dt,
   std::vector<cd> Fprev(static_cast<size_t>(n));
   std::vector<double> dW(static_cast<size_t>(n), 0.0), dA(static_cast<size_t>(n), 0.0);
   int64_t i_step = 0, i_frame = 0;
+  std::mt19937 gen(seed);  // noise_mode 3 (the reference's generator, TWMCBaseSolver.cpp:119)
   if (store_initial && n_frames > 0) {
     if (frames_ri) std::memcpy(frames_ri, beta, sizeof(cd) * size_t(n));
     if (thermo) {
@@ -373,6 +432,15 @@ static int square_run(int64_t nx, int64_t ny, double J, double gamma, double dt,
     if (noise_mode == 0) {
       const cd* src = reinterpret_cast<const cd*>(xi_ri) + i_step * n;
       for (int64_t i = 0; i < n; ++i) xi[size_t(i)] = src[i];
+    } else if (noise_mode == 3) {
+      // randCMat (TWMCBaseSolver.cpp:285-291): the distribution is passed by
+      // value, so each step starts a fresh std::normal_distribution on the
+      // trajectory's std::mt19937
+      std::normal_distribution<double> nd(0.0, 1.0);
+      for (int64_t i = 0; i < n; ++i) {
+        const double re = nd(gen);
+        xi[size_t(i)] = cd(re, nd(gen));
+      }
     } else {
       for (int64_t i = 0; i < n; ++i)
         xi[size_t(i)] = site_normal(seed, tid, uint32_t(i_step), kStreamWiener, i, n, noise_mode == 2);
@@ -493,6 +561,7 @@ int orc_lieb_run(int64_t ncell, int pbc, double J_AB, double J_BC, double detuni
   const double dt4 = std::sqrt(gamma * dt / 4.0);
   std::vector<cd> bc(static_cast<size_t>(n)), a(static_cast<size_t>(n)), xi(static_cast<size_t>(n));
   int64_t i_step = 0, i_frame = 0;
+  std::mt19937 gen(seed);  // noise_mode 3 (the reference's generator, TWMCLiebSolver.cpp:136)
   cd* frames = reinterpret_cast<cd*>(frames_ri);
   if (store_initial && n_frames > 0) {
     if (frames) std::memcpy(frames, beta, sizeof(cd) * size_t(n));
@@ -512,6 +581,15 @@ int orc_lieb_run(int64_t ncell, int pbc, double J_AB, double J_BC, double detuni
     if (noise_mode == 0) {
       const cd* src = reinterpret_cast<const cd*>(xi_ri) + i_step * n;
       for (int64_t i = 0; i < n; ++i) xi[size_t(i)] = src[i];
+    } else if (noise_mode == 3) {
+      // randCMat (TWMCBaseSolver.cpp:285-291): the distribution is passed by
+      // value, so each step starts a fresh std::normal_distribution on the
+      // trajectory's std::mt19937
+      std::normal_distribution<double> nd(0.0, 1.0);
+      for (int64_t i = 0; i < n; ++i) {
+        const double re = nd(gen);
+        xi[size_t(i)] = cd(re, nd(gen));
+      }
     } else {
       for (int64_t i = 0; i < n; ++i)
         xi[size_t(i)] = site_normal(seed, tid, uint32_t(i_step), kStreamWiener, i, n, noise_mode == 2);
@@ -582,14 +660,16 @@ void orc_disorder(int64_t n, int kind, const double* base_ri, const double* amp_
 // ---------------------------------------------------------------------------
 // Threaded CPU baseline: one trajectory per task on a pool of worker threads
 // (the reference's ThreadedTaskProcessor gives each worker thread one solver
-// and one trajectory at a time). Philox FP64 noise, vacuum-style initial
-// field supplied by the caller (same for all trajectories), frames discarded.
+// and one trajectory at a time). noise_mode 1: the Philox FP64 stream of the
+// GPU solver; 3: the reference's own generator (std::mt19937 seeded per
+// trajectory, std::normal_distribution per step). Vacuum-style initial field
+// supplied by the caller (same for all trajectories), frames discarded.
 // Returns the number of trajectories completed.
 // ---------------------------------------------------------------------------
 int64_t orc_base_run_batch(int64_t nx, int64_t ny, double J, double gamma, double dt, double t_start, double t_end,
                            int64_t frame_steps, int64_t n_frames, const double* omega_ri, const double* U_ri,
                            const double* F_ri, const double* beta0_ri, int64_t ntraj, uint32_t seed0, int nthreads,
-                           double* final_ri) {
+                           double* final_ri, int noise_mode) {
   const int64_t n = nx * ny;
   std::atomic<int64_t> next(0), done(0);
   auto worker = [&]() {
@@ -600,7 +680,7 @@ int64_t orc_base_run_batch(int64_t nx, int64_t ny, double J, double gamma, doubl
       if (k >= ntraj) break;
       std::memcpy(beta.data(), beta0_ri, sizeof(double) * size_t(2 * n));
       orc_base_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, 0, omega_ri, U_ri, F_ri,
-                   beta.data(), 1, nullptr, seed0 + uint32_t(k), uint32_t(k), nullptr, meta);
+                   beta.data(), noise_mode == 3 ? 3 : 1, nullptr, seed0 + uint32_t(k), uint32_t(k), nullptr, meta);
       if (final_ri) std::memcpy(final_ri + 2 * n * k, beta.data(), sizeof(double) * size_t(2 * n));
       done.fetch_add(1);
     }

@@ -1,23 +1,28 @@
 // twmc_hbatch.cu -- heterogeneous batch: parameter points of different
-// lattice sizes advanced together, one persistent launch per frame.
+// lattice sizes advanced together, one CUDA graph per frame.
 //
 // Each point is a square lattice (1-D chain or 2-D) with uniform parameters
-// and its own trajectories. Points whose shape has a register-FFT plan that
-// fits 256 threads per CTA run inside hbatch_kernel: a persistent kernel whose
-// CTAs take (point, trajectory group) work items from an atomic counter and
-// run the square-lattice step body for that point (tables and arguments are
-// reloaded into shared memory when the point changes). Other points (and
-// points the autotuner assigns to the real-space kernel) run through
-// ell_kernel_dev on a second stream. One frame -- counter reset, the
-// persistent launch, the real-space launches, the batched FP64 moments and the
-// advance of every point's Philox step counter -- is captured once into a CUDA
-// graph and replayed per frame; the per-point arguments live in device memory
-// so the replayed graph needs no updates.
+// and its own trajectories, and takes one step variant: the register FFT
+// (plans of 32..1024-site chains and 16x16, 32x32, 64x64), the real-space
+// stencil with 2, 4 or 8 sites per thread, row runs of four sites, or the
+// 2-CTA cluster stencil above 4096 sites. Every (point, trajectory group) is
+// a work item of a persistent work-queue kernel -- one per CTA geometry:
+// hbatch_kernel (256 threads), hbatch_kernel_512 and hbatch_cluster_kernel
+// (2-CTA clusters of 1024 threads) -- whose CTAs take items from an atomic
+// counter, longest item first, and run the variant's step body for that
+// point (arguments and tables reloaded into shared memory when the point
+// changes). One frame -- counter reset, the three queues on parallel graph
+// branches, the batched FP64 moments and the advance of every point's
+// Philox step counter -- is captured once into a CUDA graph and replayed per
+// frame; the per-point arguments live in device memory so the replayed graph
+// needs no updates.
 //
-// Autotuner: for every shape that both paths can run, the first batch that
-// needs it times the FFT kernel and the real-space kernel on a trial batch and
-// keeps the faster; choices are cached per device and shape in a JSON file
-// ($TWMC_TUNE_CACHE, default ~/.cache/twmc_tune.json).
+// Autotuner: for every shape, the first batch that needs it times each
+// variant the shape admits (FFT plan, real-space stencil with 2 / 4 / 8
+// sites per thread -- i.e. trajectories per CTA --, row runs, cluster forms)
+// on a trial batch of that point alone and keeps the fastest; choices are
+// cached per device and shape in a JSON file ($TWMC_TUNE_CACHE, default
+// ~/.cache/twmc_tune.json).
 #include <algorithm>
 #include <cmath>
 #include <complex>
@@ -39,9 +44,6 @@
 
 namespace twmc {
 
-bool ell_prepare(int prec, StepArgs* a, int* variant, int* grid, size_t* smem, std::string* err);
-bool ell_launch_dev(int prec, int variant, int hop, const StepArgs* dev_args, int grid, size_t smem, cudaStream_t s,
-                    std::string* err);
 
 namespace {
 
@@ -96,36 +98,119 @@ __device__ __forceinline__ void hb_run(unsigned char* smem, const StepArgs& a, b
   g.run(a, group, buf);
 }
 
+// Step variants of a batch point. Each runs in one of three persistent
+// work-queue kernels, by CTA geometry: 256 threads (register-FFT plans and
+// real-space stencils with 2, 4 or 8 sites per thread), 512 threads (row
+// runs, 8 sites per thread) and 2-CTA clusters of 1024 threads (lattices
+// above 4096 sites).
+enum HbVariant : int {
+  kVarFft = 0, kVarEll2, kVarEll4, kVarEll8, kVarRowrun, kVarEll8w, kVarClusterPow2, kVarCluster, kVarCount
+};
+constexpr const char* kVarName[kVarCount] = {"fft", "ell2", "ell4", "ell8", "rowrun", "ell8w", "cluster_pow2",
+                                             "cluster"};
+enum HbQueue : int { kQ256 = 0, kQ512, kQCluster, kQueues };
+constexpr int kVarQueue[kVarCount] = {kQ256, kQ256, kQ256, kQ256, kQ512, kQ512, kQCluster, kQCluster};
+constexpr int kQueueCta[kQueues] = {256, 512, 1024};
+constexpr int64_t kOneGroup = int64_t(1) << 62;  // group stride past any batch: a body runs exactly one group
+
+// Fetches the next work item (point, trajectory group) of a queue into
+// s_item; returns false when the queue is empty. Copies the point's step
+// arguments into shared memory when the point changes.
+__device__ __forceinline__ bool hb_next(const StepArgs* __restrict__ pts, const int2* __restrict__ items, int nitems,
+                                        int* __restrict__ counter, StepArgs& s_a, int& s_item, int& cur, int2& w,
+                                        bool& reload) {
+  __syncthreads();  // the previous item is done with the shared arguments and buffers
+  if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+  __syncthreads();
+  const int it = s_item;
+  if (it >= nitems) return false;
+  w = items[it];
+  reload = w.x != cur;
+  if (reload) {
+    for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += blockDim.x)
+      reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(pts + w.x)[i];
+    __syncthreads();
+    cur = w.x;
+  }
+  return true;
+}
+
+// 256-thread queue: register-FFT plans and real-space stencils.
 __global__ void __launch_bounds__(HB_CTA, 2)
-hbatch_kernel(const StepArgs* __restrict__ pts, const int* __restrict__ pshape, const int2* __restrict__ items,
-              int nitems, int* __restrict__ counter) {
+hbatch_kernel(const StepArgs* __restrict__ pts, const int* __restrict__ pvar, const int* __restrict__ pshape,
+              const int2* __restrict__ items, int nitems, int* __restrict__ counter) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) StepArgs s_a;
+  __shared__ int s_item;
+  int cur = -1, buf = 0;
+  int2 w;
+  bool reload;
+  while (hb_next(pts, items, nitems, counter, s_a, s_item, cur, w, reload)) {
+    switch (pvar[w.x]) {
+      case kVarFft:
+        switch (pshape[w.x]) {
+#define TWMC_HB_CASE(BX, BY) \
+  case kShape_##BX##_##BY: hb_run<Plan_##BX##_##BY>(smem_raw, s_a, reload, w.y, buf); break;
+          TWMC_HB_SHAPES(TWMC_HB_CASE)
+#undef TWMC_HB_CASE
+          default: break;
+        }
+        break;
+      case kVarEll2: ell_body<float, 2, HB_CTA, 1, true>(s_a, smem_raw, w.y, kOneGroup); break;
+      case kVarEll4: ell_body<float, 4, HB_CTA, 1, true>(s_a, smem_raw, w.y, kOneGroup); break;
+      case kVarEll8: ell_body<float, 8, HB_CTA, 1, true>(s_a, smem_raw, w.y, kOneGroup); break;
+      default: break;
+    }
+  }
+}
+
+// 512-thread queue: row runs of four sites and the 8-site real-space stencil.
+__global__ void __launch_bounds__(512, 1)
+hbatch_kernel_512(const StepArgs* __restrict__ pts, const int* __restrict__ pvar, const int2* __restrict__ items,
+                  int nitems, int* __restrict__ counter) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
   __shared__ __align__(16) StepArgs s_a;
   __shared__ int s_item;
   int cur = -1;
-  int buf = 0;
+  int2 w;
+  bool reload;
+  while (hb_next(pts, items, nitems, counter, s_a, s_item, cur, w, reload)) {
+    if (pvar[w.x] == kVarRowrun) rowrun_body<512>(s_a, smem_raw, w.y, kOneGroup);
+    else ell_body<float, 8, 512, 1, true>(s_a, smem_raw, w.y, kOneGroup);
+  }
+}
+
+// Cluster queue: one item is one trajectory, run by both CTAs of a 2-CTA
+// cluster; rank 0 takes the item and rank 1 reads it through distributed
+// shared memory, so both ranks leave the loop together.
+__global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(1024, 1)
+hbatch_cluster_kernel(const StepArgs* __restrict__ pts, const int* __restrict__ pvar,
+                      const int2* __restrict__ items, int nitems, int* __restrict__ counter) {
+  namespace cg = cooperative_groups;
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  __shared__ __align__(16) StepArgs s_a;
+  __shared__ int s_item;
+  cg::cluster_group cl = cg::this_cluster();
+  const unsigned rank = cl.block_rank();
+  int cur = -1;
   for (;;) {
-    __syncthreads();  // the previous item is done with the tables and arguments
-    if (threadIdx.x == 0) s_item = atomicAdd(counter, 1);
-    __syncthreads();
-    const int it = s_item;
+    cl.sync();  // both ranks are done with the previous item (buffers, peer reads, s_item)
+    if (rank == 0 && threadIdx.x == 0) s_item = atomicAdd(counter, 1);
+    cl.sync();
+    const int it = rank == 0 ? s_item : *cl.map_shared_rank(&s_item, 0);
     if (it >= nitems) break;
     const int2 w = items[it];
-    const bool reload = w.x != cur;
-    if (reload) {
-      for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += HB_CTA)
+    if (w.x != cur) {
+      __syncthreads();
+      for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += 1024)
         reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(pts + w.x)[i];
       __syncthreads();
       cur = w.x;
     }
-    switch (pshape[w.x]) {
-#define TWMC_HB_CASE(BX, BY) \
-  case kShape_##BX##_##BY: hb_run<Plan_##BX##_##BY>(smem_raw, s_a, reload, w.y, buf); break;
-      TWMC_HB_SHAPES(TWMC_HB_CASE)
-#undef TWMC_HB_CASE
-      default: break;
-    }
+    if (pvar[w.x] == kVarClusterPow2) ell_cluster_pow2_body<1024, true>(s_a, smem_raw, w.y, kOneGroup);
+    else ell_cluster_body<float, 1024>(s_a, smem_raw, w.y, kOneGroup);
   }
+  cl.sync();  // rank 0's shared memory stays until rank 1 has read the last item index
 }
 
 // FP64 moment blocks of every point: grid (site chunk, block, point).
@@ -212,7 +297,7 @@ std::string tune_cache_path() {
   return std::string(home ? home : ".") + "/.cache/twmc_tune.json";
 }
 
-// cache: one line per entry: "<device>|<bx>x<by>": "fft"|"ell"
+// cache: one line per entry: "<device>|<nx>x<ny>": "<variant name>"
 std::map<std::string, std::string> read_cache(const std::string& path) {
   std::map<std::string, std::string> m;
   std::ifstream f(path);
@@ -247,25 +332,22 @@ std::mutex g_tune_mu;
 using namespace twmc;
 using cd = std::complex<double>;
 
-constexpr int kEllStreams = 8;
-
 struct twmc_hbatch {
   int device = 0;
-  cudaStream_t s0 = nullptr, s1 = nullptr;
-  cudaEvent_t fork = nullptr, join = nullptr, e0 = nullptr, e1 = nullptr;
-  // real-space points run on kEllStreams captured streams (parallel graph
-  // branches), so that small points do not serialise behind each other
-  std::vector<cudaStream_t> ell_streams;
-  std::vector<cudaEvent_t> ell_joins;
+  cudaStream_t s0 = nullptr;
+  // the 512-thread and cluster queues run on their own captured streams,
+  // parallel graph branches beside the 256-thread queue on s0
+  cudaStream_t sq[kQueues] = {nullptr, nullptr, nullptr};
+  cudaEvent_t fork = nullptr, e0 = nullptr, e1 = nullptr;
+  cudaEvent_t qjoin[kQueues] = {nullptr, nullptr, nullptr};
   std::string err;
   int64_t frame_steps = 1;
   size_t npts = 0;
   std::vector<twmc_point_desc> desc;
-  std::vector<int> shape;          // persistent-kernel shape id, or -1 (real-space kernel)
+  std::vector<int> var;            // step variant (HbVariant) per point
+  std::vector<int> shape;          // register-FFT plan id per point (kVarFft), else -1
   std::vector<std::string> plan;
   std::vector<int64_t> nsites, ntraj, off_state, nblocks;
-  std::vector<int> ell_variant, ell_grid;
-  std::vector<size_t> ell_smem;
   DBuf<float2> state;
   DBuf<float> nk;
   DBuf<uint32_t> seeds, ids;
@@ -273,9 +355,11 @@ struct twmc_hbatch {
   DBuf<float2> tw;
   DBuf<float> kt;
   DBuf<StepArgs> args;
-  DBuf<int> pshape;
-  DBuf<int2> items;
-  DBuf<int> counter;
+  DBuf<int> pvar, pshape;
+  DBuf<int2> qitems[kQueues];
+  int qn[kQueues] = {0, 0, 0}, qgrid[kQueues] = {0, 0, 0};
+  size_t qsmem[kQueues] = {0, 0, 0};
+  DBuf<int> counter;               // one work counter per queue
   DBuf<MomentArgs> margs;
   DBuf<double> moments;
   std::vector<int64_t> mom_off;
@@ -285,7 +369,6 @@ struct twmc_hbatch {
   DBuf<int64_t> blk_off;           // first moment block of each point in the block-mean output
   DBuf<double> blk_means;
   int64_t total_blocks = 0;
-  int nitems = 0, grid = 0;
   int64_t max_sites = 0;
   int max_blocks = 0;
   cudaGraph_t graph = nullptr;
@@ -364,16 +447,100 @@ void fill_args(const twmc_hbatch* b, size_t i, StepArgs* a) {
   a->f_J = float(d.J);
 }
 
-}  // namespace
 
-extern "C" {
+// Whether variant v can run point d (N = nx ny sites, all FP32 fast runs:
+// Philox noise, uniform parameters).
+bool var_ok(int v, const twmc_point_desc& d) {
+  const int64_t n = d.nx * d.ny, half = (n + 1) / 2;
+  const int bx = lg2(d.nx), by = lg2(d.ny);
+  switch (v) {
+    case kVarFft: return bx >= 0 && by >= 0 && hb_shape_id(bx, by) >= 0;
+    case kVarEll2: return (half + 0) / 1 <= HB_CTA;
+    case kVarEll4: return (half + 1) / 2 <= HB_CTA;
+    case kVarEll8: return (half + 3) / 4 <= HB_CTA;
+    case kVarRowrun: return n <= 4096 && n % 8 == 0 && d.ny % 4 == 0;
+    case kVarEll8w: return (half + 3) / 4 <= 512;
+    case kVarClusterPow2:
+      return n > 4096 && n <= 16384 && (n & (n - 1)) == 0 && d.ny >= 2 && (d.ny & (d.ny - 1)) == 0 && d.ny <= n / 4;
+    case kVarCluster: return n > 4096 && n <= 16384;
+    default: return false;
+  }
+}
 
-int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_steps, int32_t tune, twmc_hbatch** out) {
-  if (!out) return TWMC_ERR_INVALID;
-  *out = nullptr;
-  twmc_hbatch* b = new (std::nothrow) twmc_hbatch();
-  if (!b) return TWMC_ERR_NOMEM;
-  *out = b;
+// Threads per trajectory of the real-space variants, and trajectories per
+// work item of every variant.
+int var_tpt(int v, int64_t n) {
+  const int64_t half = (n + 1) / 2;
+  switch (v) {
+    case kVarEll2: return int(half);
+    case kVarEll4: return int((half + 1) / 2);
+    case kVarEll8: case kVarEll8w: return int((half + 3) / 4);
+    case kVarRowrun: return int(n / 8);
+    default: return 0;
+  }
+}
+int var_tpc(int v, const twmc_point_desc& d, int shape) {
+  if (v == kVarFft) return hb_tpc(shape);
+  if (v == kVarClusterPow2 || v == kVarCluster) return 1;
+  return kQueueCta[kVarQueue[v]] / var_tpt(v, d.nx * d.ny);
+}
+// Dynamic shared memory of one item of variant v.
+size_t var_smem(int v, const twmc_point_desc& d, int shape) {
+  const int64_t n = d.nx * d.ny;
+  if (v == kVarFft) return kHbSmem;
+  if (v == kVarClusterPow2 || v == kVarCluster) {
+    const int64_t half = (n + 1) / 2, q = (half + 1) / 2;
+    return sizeof(float2) * 4 * size_t(q);
+  }
+  return ell_state_bytes(true, var_tpc(v, d, shape), n, sizeof(float2));
+}
+
+// The variant a point takes without tuning: the register FFT where a plan
+// exists; else, up to 4096 sites, row runs on 4096-site lattices and
+// otherwise the real-space stencil with the fewest idle site slots; above
+// 4096 sites the cluster stencil (power-of-two geometry where it applies).
+int default_var(const twmc_point_desc& d) {
+  if (var_ok(kVarFft, d)) return kVarFft;
+  const int64_t n = d.nx * d.ny;
+  if (n > 4096) return var_ok(kVarClusterPow2, d) ? kVarClusterPow2 : kVarCluster;
+  if (n == 4096 && var_ok(kVarRowrun, d)) return kVarRowrun;
+  int best = kVarEll8w;
+  double best_u = -1.0;
+  for (int v : {kVarEll2, kVarEll4, kVarEll8, kVarEll8w}) {
+    if (!var_ok(v, d)) continue;
+    const int vpt = v == kVarEll2 ? 2 : v == kVarEll4 ? 4 : 8;
+    const int cta = kQueueCta[kVarQueue[v]];
+    const int64_t tpc = cta / var_tpt(v, n);
+    const double u = double(n * tpc) / double(int64_t(cta) * vpt);
+    if (u > best_u + 1e-9) { best_u = u; best = v; }
+  }
+  return best;
+}
+
+int hb_build(twmc_hbatch* b, const twmc_point_desc* points, size_t n, int64_t frame_steps, const int* forced,
+             int32_t tune);
+
+// Site-updates per second of variant v on point d alone: a trial batch of
+// the point (at most 2048 trajectories), one untimed 50-step frame, then two
+// timed frames.
+double trial_rate(const twmc_point_desc& d, int v) {
+  twmc_point_desc t = d;
+  t.n_traj = std::min<int64_t>(std::max<int64_t>(d.n_traj, 256), 2048);
+  t.n_moment_blocks = 1;
+  twmc_hbatch* tb = new (std::nothrow) twmc_hbatch();
+  if (!tb) return 0.0;
+  double rate = 0.0;
+  double ms = 0.0;
+  if (hb_build(tb, &t, 1, 50, &v, 0) == TWMC_OK && twmc_hbatch_run(tb, 1) == TWMC_OK &&
+      twmc_hbatch_sync(tb, nullptr) == TWMC_OK && twmc_hbatch_run(tb, 2) == TWMC_OK &&
+      twmc_hbatch_sync(tb, &ms) == TWMC_OK && ms > 0)
+    rate = double(t.n_traj) * 100.0 * double(t.nx * t.ny) / (ms * 1e-3);
+  twmc_hbatch_destroy(tb);
+  return rate;
+}
+
+int hb_build(twmc_hbatch* b, const twmc_point_desc* points, size_t n, int64_t frame_steps, const int* forced,
+             int32_t tune) {
   if (!points || n == 0) return hfail(b, TWMC_ERR_INVALID, "no points");
   if (frame_steps < 1) return hfail(b, TWMC_ERR_INVALID, "frame_steps must be >= 1");
   cudaGetDevice(&b->device);
@@ -385,18 +552,13 @@ int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_st
     if (d.nx < 1 || d.ny < 1 || d.n_traj < 1 || !(d.dt > 0) || d.gamma < 0 || d.n_moment_blocks < 0)
       return hfail(b, TWMC_ERR_INVALID, "point " + std::to_string(i) + ": invalid parameters");
     if (d.nx * d.ny > 16384) return hfail(b, TWMC_ERR_INVALID, "point " + std::to_string(i) + ": more than 16384 sites");
+    if (d.n_traj > (int64_t(1) << 30)) return hfail(b, TWMC_ERR_INVALID, "point " + std::to_string(i) + ": too many trajectories");
   }
   cudaStreamCreateWithFlags(&b->s0, cudaStreamNonBlocking);
-  cudaStreamCreateWithFlags(&b->s1, cudaStreamNonBlocking);
   cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming);
-  cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming);
-  b->ell_streams.assign(kEllStreams, nullptr);
-  b->ell_joins.assign(kEllStreams, nullptr);
-  b->ell_streams[0] = b->s1;
-  b->ell_joins[0] = b->join;
-  for (int k = 1; k < kEllStreams; ++k) {
-    cudaStreamCreateWithFlags(&b->ell_streams[k], cudaStreamNonBlocking);
-    cudaEventCreateWithFlags(&b->ell_joins[k], cudaEventDisableTiming);
+  for (int q = 0; q < kQueues; ++q) {
+    cudaStreamCreateWithFlags(&b->sq[q], cudaStreamNonBlocking);
+    cudaEventCreateWithFlags(&b->qjoin[q], cudaEventDisableTiming);
   }
   cudaEventCreate(&b->e0);
   cudaEventCreate(&b->e1);
@@ -404,65 +566,44 @@ int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_st
   cudaGetDeviceProperties(&prop, b->device);
   const std::string devname = prop.name;
 
-  // kernel per point: persistent FFT kernel where a plan exists (subject to the
-  // autotuner), real-space kernel otherwise
+  // step variant per point: forced, tuned (per shape, cached) or the default
+  b->var.assign(n, -1);
   b->shape.assign(n, -1);
-  b->plan.assign(n, "ell_kernel<stencil>");
+  b->plan.assign(n, "");
   std::map<std::string, std::string> cache;
   const std::string cpath = tune_cache_path();
   if (tune) cache = read_cache(cpath);
   bool cache_dirty = false;
   for (size_t i = 0; i < n; ++i) {
-    const int bx = lg2(points[i].nx), by = lg2(points[i].ny);
-    const int sid = (bx >= 0 && by >= 0) ? hb_shape_id(bx, by) : -1;
-    if (sid < 0) continue;
-    std::string choice = "fft";
-    if (tune) {
-      const std::string key = devname + "|" + std::to_string(points[i].nx) + "x" + std::to_string(points[i].ny);
+    const twmc_point_desc& d = points[i];
+    int v = forced ? forced[i] : default_var(d);
+    if (!forced && tune) {
+      const std::string key = devname + "|" + std::to_string(d.nx) + "x" + std::to_string(d.ny);
       std::lock_guard<std::mutex> lock(g_tune_mu);
       auto it = cache.find(key);
-      if (it != cache.end()) {
-        choice = it->second;
+      int cached = -1;
+      if (it != cache.end())
+        for (int k = 0; k < kVarCount; ++k) if (it->second == kVarName[k] && var_ok(k, d)) cached = k;
+      if (cached >= 0) {
+        v = cached;
       } else {
-        // trial: both kernels on up to 1024 trajectories, 50 steps
-        twmc_system_desc sd;
-        std::memset(&sd, 0, sizeof(sd));
-        sd.lattice = TWMC_LATTICE_SQUARE;
-        sd.nx = points[i].nx;
-        sd.ny = points[i].ny;
-        sd.J = points[i].J;
-        sd.gamma = points[i].gamma;
-        sd.dt = points[i].dt;
-        sd.frame_steps = 50;
-        double rate[2] = {0, 0};
-        for (int hop = 0; hop < 2; ++hop) {
-          sd.hop_mode = hop;
-          twmc_handle* h = nullptr;
-          if (twmc_create(&sd, &h) != TWMC_OK) { twmc_destroy(h); continue; }
-          const int64_t nt = std::min<int64_t>(1024, std::max<int64_t>(points[i].n_traj, 64));
-          std::vector<twmc_task_desc> td(static_cast<size_t>(nt));
-          for (int64_t k = 0; k < nt; ++k) {
-            std::memset(&td[size_t(k)], 0, sizeof(twmc_task_desc));
-            td[size_t(k)].id = uint64_t(k + 1);
-            td[size_t(k)].seed = uint32_t(k + 7);
-            td[size_t(k)].ic_kind = TWMC_IC_FIXED;
-          }
-          double ms = 0;
-          if (twmc_batch_init(h, td.data(), td.size()) == TWMC_OK && twmc_batch_advance(h, 10) == TWMC_OK &&
-              twmc_sync(h, &ms) == TWMC_OK && twmc_batch_advance(h, 50) == TWMC_OK && twmc_sync(h, &ms) == TWMC_OK &&
-              ms > 0)
-            rate[hop] = double(nt) * 50.0 * double(sd.nx * sd.ny) / (ms * 1e-3);
-          twmc_destroy(h);
+        double best = -1.0;
+        for (int k = 0; k < kVarCount; ++k) {
+          if (!var_ok(k, d)) continue;
+          const double r = trial_rate(d, k);
+          if (r > best) { best = r; v = k; }
         }
-        choice = rate[1] > rate[0] ? "ell" : "fft";
-        cache[key] = choice;
+        cache[key] = kVarName[v];
         cache_dirty = true;
       }
     }
-    if (choice == "fft") {
-      b->shape[i] = sid;
-      b->plan[i] = "hbatch_kernel<" + std::to_string(points[i].nx) + "x" + std::to_string(points[i].ny) + ">";
-    }
+    if (v < 0 || v >= kVarCount || !var_ok(v, d))
+      return hfail(b, TWMC_ERR_INVALID, "point " + std::to_string(i) + ": no step variant for this lattice");
+    b->var[i] = v;
+    if (v == kVarFft) b->shape[i] = hb_shape_id(lg2(d.nx), lg2(d.ny));
+    static const char* qname[kQueues] = {"hbatch_kernel", "hbatch_kernel_512", "hbatch_cluster_kernel"};
+    b->plan[i] = std::string(qname[kVarQueue[v]]) + "<" + kVarName[v] + " " + std::to_string(d.nx) + "x" +
+                 std::to_string(d.ny) + ">";
   }
   if (cache_dirty) write_cache(cpath, cache);
   cudaSetDevice(b->device);
@@ -536,52 +677,58 @@ int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_st
     }
     to += d.n_traj;
   }
-  if (!b->tw.alloc(tw.size()) || !b->kt.alloc(kt.size()) || !b->args.alloc(n) || !b->pshape.alloc(n) ||
-      !b->counter.alloc(1) || !b->margs.alloc(n))
+  if (!b->tw.alloc(tw.size()) || !b->kt.alloc(kt.size()) || !b->args.alloc(n) || !b->pvar.alloc(n) ||
+      !b->pshape.alloc(n) || !b->counter.alloc(kQueues) || !b->margs.alloc(n))
     return hfail(b, TWMC_ERR_NOMEM, "device allocation failed");
   cudaMemcpy(b->tw.p, tw.data(), tw.size() * sizeof(float2), cudaMemcpyHostToDevice);
   cudaMemcpy(b->kt.p, kt.data(), kt.size() * sizeof(float), cudaMemcpyHostToDevice);
   cudaMemcpy(b->seeds.p, hseeds.data(), hseeds.size() * 4, cudaMemcpyHostToDevice);
   cudaMemcpy(b->ids.p, hids.data(), hids.size() * 4, cudaMemcpyHostToDevice);
+  cudaMemcpy(b->pvar.p, b->var.data(), n * sizeof(int), cudaMemcpyHostToDevice);
   cudaMemcpy(b->pshape.p, b->shape.data(), n * sizeof(int), cudaMemcpyHostToDevice);
-  // arguments, real-space launch configurations, work items, moment args
+  // arguments, work items (longest item first in every queue), moment args
   std::vector<StepArgs> hargs(n);
   std::vector<MomentArgs> hm(n);
-  std::vector<int2> hitems;
-  b->ell_variant.assign(n, -1);
-  b->ell_grid.assign(n, 0);
-  b->ell_smem.assign(n, 0);
+  std::vector<std::pair<double, size_t>> order[kQueues];
   for (size_t i = 0; i < n; ++i) {
     StepArgs& a = hargs[i];
     fill_args(b, i, &a);
+    const int v = b->var[i];
     a.state = b->state.p + b->off_state[i];
     a.seeds = b->seeds.p + traj_off[i];
     a.ids = b->ids.p + traj_off[i];
     a.status = b->status.p + traj_off[i];
-    a.nk = b->nk.p + b->off_state[i];
+    a.nk = v == kVarFft ? b->nk.p + b->off_state[i] : nullptr;  // k-space populations from the FFT only
     a.tw = b->tw.p + tw_off[i];
     a.ktab = b->kt.p + tw_off[i];
-    if (b->shape[i] >= 0) {
-      const int tpc = hb_tpc(b->shape[i]);
-      for (int64_t g = 0; g < (b->ntraj[i] + tpc - 1) / tpc; ++g) hitems.push_back(make_int2(int(i), int(g)));
-    } else {
-      a.nk = nullptr;  // the real-space kernel has no k-space output
-      std::string e;
-      if (!ell_prepare(0, &a, &b->ell_variant[i], &b->ell_grid[i], &b->ell_smem[i], &e))
-        return hfail(b, TWMC_ERR_INVALID, "point " + std::to_string(i) + ": " + e);
-    }
+    a.tpt = var_tpt(v, b->nsites[i]);
+    a.dbuf = 1;
+    const int q = kVarQueue[v];
+    const int tpc = var_tpc(v, points[i], b->shape[i]);
+    order[q].push_back({double(b->nsites[i]) * double(tpc), i});
+    b->qsmem[q] = std::max(b->qsmem[q], var_smem(v, points[i], b->shape[i]));
     MomentArgs& m = hm[i];
     m.ntraj = b->ntraj[i];
     m.nsites = b->nsites[i];
     m.prec = 0;
     m.state = a.state;
-    m.nk = b->shape[i] >= 0 ? a.nk : nullptr;
+    m.nk = a.nk;
     m.nblocks = int(b->nblocks[i]);
     m.out = b->moments.p + b->mom_off[i];
   }
-  b->nitems = int(hitems.size());
-  if (!b->items.alloc(std::max<size_t>(hitems.size(), 1))) return hfail(b, TWMC_ERR_NOMEM, "device allocation failed");
-  if (!hitems.empty()) cudaMemcpy(b->items.p, hitems.data(), hitems.size() * sizeof(int2), cudaMemcpyHostToDevice);
+  for (int q = 0; q < kQueues; ++q) {
+    std::stable_sort(order[q].begin(), order[q].end(),
+                     [](const std::pair<double, size_t>& x, const std::pair<double, size_t>& y) { return x.first > y.first; });
+    std::vector<int2> items;
+    for (const auto& o : order[q]) {
+      const size_t i = o.second;
+      const int tpc = var_tpc(b->var[i], points[i], b->shape[i]);
+      for (int64_t g = 0; g < (b->ntraj[i] + tpc - 1) / tpc; ++g) items.push_back(make_int2(int(i), int(g)));
+    }
+    b->qn[q] = int(items.size());
+    if (!b->qitems[q].alloc(std::max<size_t>(items.size(), 1))) return hfail(b, TWMC_ERR_NOMEM, "device allocation failed");
+    if (!items.empty()) cudaMemcpy(b->qitems[q].p, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice);
+  }
   cudaMemcpy(b->args.p, hargs.data(), n * sizeof(StepArgs), cudaMemcpyHostToDevice);
   cudaMemcpy(b->margs.p, hm.data(), n * sizeof(MomentArgs), cudaMemcpyHostToDevice);
 
@@ -591,58 +738,99 @@ int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_st
     if (!init_point(b, i, nullptr, nullptr, &e)) return hfail(b, TWMC_ERR_CUDA, e);
   }
 
-  // persistent kernel configuration
-  if (b->nitems > 0) {
-    cudaError_t e = cudaFuncSetAttribute(hbatch_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(kHbSmem));
-    if (e != cudaSuccess) { cudaGetLastError(); return hfail(b, TWMC_ERR_CUDA, std::string("hbatch smem: ") + cudaGetErrorString(e)); }
-    int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, hbatch_kernel, HB_CTA, kHbSmem);
-    b->grid = std::max(1, std::min(b->nitems, prop.multiProcessorCount * std::max(per_sm, 1)));
+  // persistent grids: every resident CTA (cluster) of the device, at most one per item
+  int maxsm = 0;
+  cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, b->device);
+  const void* qfn[kQueues] = {reinterpret_cast<const void*>(hbatch_kernel),
+                              reinterpret_cast<const void*>(hbatch_kernel_512),
+                              reinterpret_cast<const void*>(hbatch_cluster_kernel)};
+  for (int q = 0; q < kQueues; ++q) {
+    if (b->qn[q] == 0) continue;
+    const size_t smem = b->qsmem[q];
+    if (smem + sizeof(StepArgs) + 64 > size_t(maxsm)) return hfail(b, TWMC_ERR_INVALID, "batch queue: field does not fit");
+    cudaError_t e = cudaFuncSetAttribute(qfn[q], cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) { cudaGetLastError(); return hfail(b, TWMC_ERR_CUDA, std::string("batch queue smem: ") + cudaGetErrorString(e)); }
+    int slots = 0;
+    if (q == kQCluster) {
+      cudaLaunchConfig_t cfg = {};
+      cfg.gridDim = dim3(2, 1, 1);
+      cfg.blockDim = dim3(1024, 1, 1);
+      cfg.dynamicSmemBytes = smem;
+      int ncl = 0;
+      e = cudaOccupancyMaxActiveClusters(&ncl, qfn[q], &cfg);
+      if (e != cudaSuccess || ncl <= 0) { cudaGetLastError(); return hfail(b, TWMC_ERR_CUDA, "batch cluster queue does not fit"); }
+      b->qgrid[q] = 2 * std::min(b->qn[q], ncl);
+    } else {
+      e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&slots, qfn[q], kQueueCta[q], smem);
+      if (e != cudaSuccess || slots <= 0) { cudaGetLastError(); return hfail(b, TWMC_ERR_CUDA, "batch queue does not fit on an SM"); }
+      b->qgrid[q] = std::max(1, std::min(b->qn[q], prop.multiProcessorCount * slots));
+    }
   }
 
-  // capture one frame
+  // capture one frame: counters reset, the three queues on parallel
+  // branches, then the batched moments and the step-counter bump
   cudaStream_t s0 = b->s0;
   cudaStreamSynchronize(s0);
   if (cudaStreamBeginCapture(s0, cudaStreamCaptureModeThreadLocal) != cudaSuccess)
     return hfail(b, TWMC_ERR_CUDA, "stream capture failed to start");
+  cudaMemsetAsync(b->counter.p, 0, kQueues * sizeof(int), s0);
   cudaEventRecord(b->fork, s0);
-  for (cudaStream_t es : b->ell_streams) cudaStreamWaitEvent(es, b->fork, 0);
-  std::string cerr;
-  bool ok = true;
-  {
-    // longest-processing-time-first assignment of the real-space points to
-    // the least loaded stream (load = trajectories x sites)
-    std::vector<size_t> order;
-    for (size_t i = 0; i < n; ++i) if (b->shape[i] < 0) order.push_back(i);
-    std::sort(order.begin(), order.end(), [&](size_t x, size_t y) {
-      return b->ntraj[x] * b->nsites[x] > b->ntraj[y] * b->nsites[y];
-    });
-    std::vector<double> load(b->ell_streams.size(), 0.0);
-    for (size_t i : order) {
-      if (!ok) break;
-      const size_t k = size_t(std::min_element(load.begin(), load.end()) - load.begin());
-      load[k] += double(b->ntraj[i]) * double(b->nsites[i]);
-      ok = ell_launch_dev(0, b->ell_variant[i], 1, b->args.p + i, b->ell_grid[i], b->ell_smem[i],
-                          b->ell_streams[k], &cerr);
-    }
+  for (int q = 0; q < kQueues; ++q) cudaStreamWaitEvent(b->sq[q], b->fork, 0);
+  if (b->qn[kQ256] > 0)
+    hbatch_kernel<<<b->qgrid[kQ256], HB_CTA, b->qsmem[kQ256], b->sq[kQ256]>>>(
+        b->args.p, b->pvar.p, b->pshape.p, b->qitems[kQ256].p, b->qn[kQ256], b->counter.p + kQ256);
+  if (b->qn[kQ512] > 0)
+    hbatch_kernel_512<<<b->qgrid[kQ512], 512, b->qsmem[kQ512], b->sq[kQ512]>>>(
+        b->args.p, b->pvar.p, b->qitems[kQ512].p, b->qn[kQ512], b->counter.p + kQ512);
+  if (b->qn[kQCluster] > 0)
+    hbatch_cluster_kernel<<<b->qgrid[kQCluster], 1024, b->qsmem[kQCluster], b->sq[kQCluster]>>>(
+        b->args.p, b->pvar.p, b->qitems[kQCluster].p, b->qn[kQCluster], b->counter.p + kQCluster);
+  cudaError_t le = cudaGetLastError();
+  for (int q = 0; q < kQueues; ++q) {
+    cudaEventRecord(b->qjoin[q], b->sq[q]);
+    cudaStreamWaitEvent(s0, b->qjoin[q], 0);
   }
-  for (size_t k = 0; k < b->ell_streams.size(); ++k) cudaEventRecord(b->ell_joins[k], b->ell_streams[k]);
-  if (b->nitems > 0) {
-    cudaMemsetAsync(b->counter.p, 0, sizeof(int), s0);
-    hbatch_kernel<<<b->grid, HB_CTA, kHbSmem, s0>>>(b->args.p, b->pshape.p, b->items.p, b->nitems, b->counter.p);
-  }
-  for (cudaEvent_t ej : b->ell_joins) cudaStreamWaitEvent(s0, ej, 0);
   dim3 mg(unsigned((b->max_sites + 127) / 128), unsigned(b->max_blocks), unsigned(n));
   hbatch_moments_kernel<<<mg, 128, 0, s0>>>(b->margs.p);
   hbatch_bump_kernel<<<unsigned((n + 127) / 128), 128, 0, s0>>>(b->args.p, int(n), uint32_t(frame_steps));
   cudaError_t ce = cudaStreamEndCapture(s0, &b->graph);
-  if (!ok || ce != cudaSuccess) {
+  if (le != cudaSuccess || ce != cudaSuccess) {
     cudaGetLastError();
-    return hfail(b, TWMC_ERR_CUDA, "graph capture failed: " + (ok ? std::string(cudaGetErrorString(ce)) : cerr));
+    return hfail(b, TWMC_ERR_CUDA, "graph capture failed: " + std::string(cudaGetErrorString(le != cudaSuccess ? le : ce)));
   }
   ce = cudaGraphInstantiate(&b->exec, b->graph, 0);
   if (ce != cudaSuccess) { cudaGetLastError(); return hfail(b, TWMC_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(ce)); }
   return TWMC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int twmc_hbatch_create(const twmc_point_desc* points, size_t n, int64_t frame_steps, int32_t tune, twmc_hbatch** out) {
+  if (!out) return TWMC_ERR_INVALID;
+  *out = nullptr;
+  twmc_hbatch* b = new (std::nothrow) twmc_hbatch();
+  if (!b) return TWMC_ERR_NOMEM;
+  *out = b;
+  return hb_build(b, points, n, frame_steps, nullptr, tune);
+}
+
+int twmc_hbatch_create_variants(const twmc_point_desc* points, size_t n, int64_t frame_steps,
+                                const char* const* variants, twmc_hbatch** out) {
+  if (!out) return TWMC_ERR_INVALID;
+  *out = nullptr;
+  twmc_hbatch* b = new (std::nothrow) twmc_hbatch();
+  if (!b) return TWMC_ERR_NOMEM;
+  *out = b;
+  if (!points || !variants || n == 0) return hfail(b, TWMC_ERR_INVALID, "no points");
+  std::vector<int> forced(n, -1);
+  for (size_t i = 0; i < n; ++i) {
+    for (int k = 0; k < kVarCount; ++k)
+      if (variants[i] && std::strcmp(variants[i], kVarName[k]) == 0) forced[i] = k;
+    if (forced[i] < 0) return hfail(b, TWMC_ERR_INVALID, "point " + std::to_string(i) + ": unknown step variant");
+  }
+  return hb_build(b, points, n, frame_steps, forced.data(), 0);
 }
 
 int twmc_hbatch_run(twmc_hbatch* b, int64_t n_frames) {
@@ -742,13 +930,12 @@ void twmc_hbatch_destroy(twmc_hbatch* b) {
   if (b->s0) cudaStreamSynchronize(b->s0);
   if (b->exec) cudaGraphExecDestroy(b->exec);
   if (b->graph) cudaGraphDestroy(b->graph);
-  for (cudaEvent_t e : {b->fork, b->join, b->e0, b->e1}) if (e) cudaEventDestroy(e);
-  for (size_t k = 1; k < b->ell_streams.size(); ++k) {
-    if (b->ell_joins[k]) cudaEventDestroy(b->ell_joins[k]);
-    if (b->ell_streams[k]) cudaStreamDestroy(b->ell_streams[k]);
+  for (cudaEvent_t e : {b->fork, b->e0, b->e1}) if (e) cudaEventDestroy(e);
+  for (int q = 0; q < kQueues; ++q) {
+    if (b->qjoin[q]) cudaEventDestroy(b->qjoin[q]);
+    if (b->sq[q]) cudaStreamDestroy(b->sq[q]);
   }
   if (b->s0) cudaStreamDestroy(b->s0);
-  if (b->s1) cudaStreamDestroy(b->s1);
   delete b;
 }
 

@@ -561,8 +561,11 @@ __host__ __device__ __forceinline__ size_t ell_state_bytes(bool dbuf, int tpc, i
   return ((dbuf ? 2 : 1) * size_t(tpc) * size_t(n) * csize + 15) & ~size_t(15);
 }
 
+// Groups g_begin, g_begin + g_stride, ... (a grid-stride loop by default; a
+// work-queue kernel passes one group and a stride past the end).
 template <typename R, int VPT, int CTA, int HOP, bool FAST = false>
-__device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_raw) {
+__device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_raw, int64_t g_begin,
+                                         int64_t g_stride) {
   using T = c2_t<R>;
   constexpr int H = VPT / 2;
   T* s_b = reinterpret_cast<T*>(smem_raw);
@@ -618,7 +621,7 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
   const int64_t ngroups = (a.ntraj + tpc - 1) / tpc;
   const int64_t slice = N;
   int buf = 0;
-  for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+  for (int64_t g = g_begin; g < ngroups; g += g_stride) {
     const int64_t traj = g * tpc + slot;
     const bool active = in_slot && traj < a.ntraj;
     const int64_t tr = active ? traj : 0;
@@ -740,7 +743,7 @@ __device__ __forceinline__ void ell_body(const StepArgs& a, unsigned char* smem_
 template <typename R, int VPT, int CTA, int HOP, bool FAST>
 __global__ void __launch_bounds__(CTA) ell_kernel(const StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ell_body<R, VPT, CTA, HOP, FAST>(a, smem_raw);
+  ell_body<R, VPT, CTA, HOP, FAST>(a, smem_raw, blockIdx.x, gridDim.x);
 }
 
 // Same, with the arguments in device memory (kept there across the frames of a
@@ -752,7 +755,7 @@ __global__ void __launch_bounds__(CTA) ell_kernel_dev(const StepArgs* __restrict
   for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += CTA)
     reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(ap)[i];
   __syncthreads();
-  ell_body<R, VPT, CTA, HOP, FAST>(s_a, smem_raw);
+  ell_body<R, VPT, CTA, HOP, FAST>(s_a, smem_raw, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------------
@@ -768,7 +771,8 @@ __global__ void __launch_bounds__(CTA) ell_kernel_dev(const StepArgs* __restrict
 // equal the real-space kernel's.
 // ------------------------------------------------------------------------
 template <int CTA>
-__device__ __forceinline__ void rowrun_body(const StepArgs& a, unsigned char* smem_raw) {
+__device__ __forceinline__ void rowrun_body(const StepArgs& a, unsigned char* smem_raw, int64_t g_begin,
+                                            int64_t g_stride) {
   using T = float2;
   T* s_b = reinterpret_cast<T*>(smem_raw);
   const int N = int(a.nsites), half = N / 2, nx = int(a.nx), ny = int(a.ny);
@@ -795,7 +799,7 @@ __device__ __forceinline__ void rowrun_body(const StepArgs& a, unsigned char* sm
   }
   const int64_t ngroups = (a.ntraj + tpc - 1) / tpc;
   int buf = 0;
-  for (int64_t g = blockIdx.x; g < ngroups; g += gridDim.x) {
+  for (int64_t g = g_begin; g < ngroups; g += g_stride) {
     const int64_t traj = g * tpc + slot;
     const bool active = in_slot && traj < a.ntraj;
     const int64_t tr = active ? traj : 0;
@@ -865,7 +869,7 @@ __device__ __forceinline__ void rowrun_body(const StepArgs& a, unsigned char* sm
 template <int CTA>
 __global__ void __launch_bounds__(CTA, 1) rowrun_kernel(const StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  rowrun_body<CTA>(a, smem_raw);
+  rowrun_body<CTA>(a, smem_raw, blockIdx.x, gridDim.x);
 }
 
 template <int CTA>
@@ -875,7 +879,7 @@ __global__ void __launch_bounds__(CTA, 1) rowrun_kernel_dev(const StepArgs* __re
   for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += CTA)
     reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(ap)[i];
   __syncthreads();
-  rowrun_body<CTA>(s_a, smem_raw);
+  rowrun_body<CTA>(s_a, smem_raw, blockIdx.x, gridDim.x);
 }
 
 // ------------------------------------------------------------------------
@@ -1043,8 +1047,11 @@ __global__ void __launch_bounds__(CTA) lieb_cell_kernel(const StepArgs a) {
 // unrolling and 1024 threads fit 64 registers. Per-site parameters and both
 // noise modes as in the single-CTA kernel; no F(t) and no work / area.
 // ------------------------------------------------------------------------
+// Trajectories tr_begin, tr_begin + tr_stride, ... per cluster (both CTAs
+// of a cluster pass the same values).
 template <typename R, int CTA>
-__device__ __forceinline__ void ell_cluster_body(const StepArgs& a, unsigned char* smem_raw) {
+__device__ __forceinline__ void ell_cluster_body(const StepArgs& a, unsigned char* smem_raw, int64_t tr_begin,
+                                                 int64_t tr_stride) {
   namespace cg = cooperative_groups;
   using T = c2_t<R>;
   cg::cluster_group cl = cg::this_cluster();
@@ -1078,8 +1085,7 @@ __device__ __forceinline__ void ell_cluster_body(const StepArgs& a, unsigned cha
     return owner == rank ? lds_c((b ? oa1 : oa0) + uint32_t(slot) * TS, T{})
                          : ldc_c((b ? pa1 : pa0) + uint32_t(slot) * TS, T{});
   };
-  const int64_t nclusters = gridDim.x / 2;
-  for (int64_t tr = blockIdx.x / 2; tr < a.ntraj; tr += nclusters) {
+  for (int64_t tr = tr_begin; tr < a.ntraj; tr += tr_stride) {
     T* st = reinterpret_cast<T*>(a.state) + tr * N;
     const T* __restrict__ g_rsl = a.rsl ? reinterpret_cast<const T*>(a.rsl) + tr * a.par_stride : nullptr;
     const T* __restrict__ g_iU = a.iU ? reinterpret_cast<const T*>(a.iU) + tr * a.par_stride : nullptr;
@@ -1154,7 +1160,7 @@ __device__ __forceinline__ void ell_cluster_body(const StepArgs& a, unsigned cha
 template <typename R, int CTA>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(CTA, 1) ell_cluster_kernel(const StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ell_cluster_body<R, CTA>(a, smem_raw);
+  ell_cluster_body<R, CTA>(a, smem_raw, blockIdx.x / 2, gridDim.x / 2);
 }
 
 template <typename R, int CTA>
@@ -1164,7 +1170,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(CTA, 1) ell_cluster_
   for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += CTA)
     reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(ap)[i];
   __syncthreads();
-  ell_cluster_body<R, CTA>(s_a, smem_raw);
+  ell_cluster_body<R, CTA>(s_a, smem_raw, blockIdx.x / 2, gridDim.x / 2);
 }
 
 // ------------------------------------------------------------------------
@@ -1181,8 +1187,11 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(CTA, 1) ell_cluster_
 // compiled in (omega per site allowed); otherwise both noise modes and
 // per-site U, F as in ell_cluster_body.
 // ------------------------------------------------------------------------
+// Trajectories tr_begin, tr_begin + tr_stride, ... per cluster (both CTAs
+// of a cluster pass the same values).
 template <int CTA, bool FAST>
-__device__ __forceinline__ void ell_cluster_pow2_body(const StepArgs& a, unsigned char* smem_raw) {
+__device__ __forceinline__ void ell_cluster_pow2_body(const StepArgs& a, unsigned char* smem_raw, int64_t tr_begin,
+                                                      int64_t tr_stride) {
   namespace cg = cooperative_groups;
   using T = float2;
   cg::cluster_group cl = cg::this_cluster();
@@ -1207,8 +1216,7 @@ __device__ __forceinline__ void ell_cluster_pow2_body(const StepArgs& a, unsigne
   const uint32_t dn_edge[2] = {uint32_t(rank == 0 ? 0 : q), uint32_t(rank == 1 ? 0 : q)};
   const int lo0 = rank * q;
   const int t = threadIdx.x;
-  const int64_t nclusters = gridDim.x / 2;
-  for (int64_t tr = blockIdx.x / 2; tr < a.ntraj; tr += nclusters) {
+  for (int64_t tr = tr_begin; tr < a.ntraj; tr += tr_stride) {
     T* st = reinterpret_cast<T*>(a.state) + tr * N;
     const T* __restrict__ g_rsl = a.rsl ? reinterpret_cast<const T*>(a.rsl) + tr * a.par_stride : nullptr;
     const T* __restrict__ g_iU = !FAST && a.iU ? reinterpret_cast<const T*>(a.iU) + tr * a.par_stride : nullptr;
@@ -1277,7 +1285,7 @@ __device__ __forceinline__ void ell_cluster_pow2_body(const StepArgs& a, unsigne
 template <int CTA, bool FAST>
 __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(CTA, 1) ell_cluster_pow2_kernel(const StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  ell_cluster_pow2_body<CTA, FAST>(a, smem_raw);
+  ell_cluster_pow2_body<CTA, FAST>(a, smem_raw, blockIdx.x / 2, gridDim.x / 2);
 }
 
 template <int CTA, bool FAST>
@@ -1287,7 +1295,7 @@ __global__ void __cluster_dims__(2, 1, 1) __launch_bounds__(CTA, 1) ell_cluster_
   for (int i = threadIdx.x; i < int(sizeof(StepArgs) / 4); i += CTA)
     reinterpret_cast<uint32_t*>(&s_a)[i] = reinterpret_cast<const uint32_t*>(ap)[i];
   __syncthreads();
-  ell_cluster_pow2_body<CTA, FAST>(s_a, smem_raw);
+  ell_cluster_pow2_body<CTA, FAST>(s_a, smem_raw, blockIdx.x / 2, gridDim.x / 2);
 }
 
 }  // namespace twmc

@@ -30,7 +30,7 @@ EXPORTED = [
     "twmc_destroy", "twmc_batch_init", "twmc_batch_advance", "twmc_batch_reduce", "twmc_sync",
     "twmc_batch_download", "twmc_launch_count", "twmc_kernel_name", "twmc_stream", "twmc_measure_fp32_peak",
     "twmc_kspace_moments_noalloc", "twmc_debug_philox", "twmc_debug_wiener",
-    "twmc_hbatch_create", "twmc_hbatch_run", "twmc_hbatch_sync", "twmc_hbatch_moments", "twmc_hbatch_state",
+    "twmc_hbatch_create", "twmc_hbatch_create_variants", "twmc_hbatch_run", "twmc_hbatch_sync", "twmc_hbatch_moments", "twmc_hbatch_state",
     "twmc_hbatch_plan", "twmc_hbatch_last_error", "twmc_hbatch_launch_count", "twmc_hbatch_destroy",
     "twmc_hbatch_set_init", "twmc_hbatch_field_moments", "twmc_hbatch_total_sites", "twmc_hbatch_stream",
     "twmc_hbatch_block_means",
@@ -119,6 +119,8 @@ def load(path: Optional[str] = None):
     lib.twmc_stream.restype = C.c_void_p
     lib.twmc_measure_fp32_peak.argtypes = [C.POINTER(C.c_double)]
     lib.twmc_hbatch_create.argtypes = [C.POINTER(PointDesc), C.c_size_t, C.c_int64, C.c_int32, C.POINTER(C.c_void_p)]
+    lib.twmc_hbatch_create_variants.argtypes = [C.POINTER(PointDesc), C.c_size_t, C.c_int64,
+                                                C.POINTER(C.c_char_p), C.POINTER(C.c_void_p)]
     lib.twmc_hbatch_run.argtypes = [C.c_void_p, C.c_int64]
     lib.twmc_hbatch_sync.argtypes = [C.c_void_p, C.POINTER(C.c_double)]
     lib.twmc_hbatch_moments.argtypes = [C.c_void_p, C.c_size_t, C.c_void_p]
@@ -375,7 +377,11 @@ def _c2(v):
 class HBatch:
     """Heterogeneous batch of parameter points (twmc_hbatch_*)."""
 
-    def __init__(self, points, frame_steps: int, tune: bool = False):
+    VARIANTS = ("fft", "ell2", "ell4", "ell8", "rowrun", "ell8w", "cluster_pow2", "cluster")
+
+    def __init__(self, points, frame_steps: int, tune: bool = False, variants: Optional[Sequence[str]] = None):
+        """variants: a step variant name per point (twmc_hbatch_create_variants);
+        None = the default choice, or the autotuner's with tune=True."""
         self.lib = load()
         arr = (PointDesc * len(points))()
         self.n_sites = []
@@ -393,7 +399,11 @@ class HBatch:
             self.n_traj.append(d.n_traj)
             self.n_blocks.append(min(d.n_moment_blocks or 32, d.n_traj))
         h = C.c_void_p()
-        rc = self.lib.twmc_hbatch_create(arr, len(points), frame_steps, int(tune), C.byref(h))
+        if variants is not None:
+            names = (C.c_char_p * len(points))(*[v.encode() for v in variants])
+            rc = self.lib.twmc_hbatch_create_variants(arr, len(points), frame_steps, names, C.byref(h))
+        else:
+            rc = self.lib.twmc_hbatch_create(arr, len(points), frame_steps, int(tune), C.byref(h))
         self.h = h
         if rc != OK:
             msg = self.lib.twmc_hbatch_last_error(h).decode() if h else ""

@@ -8,9 +8,9 @@ trajectory then starts from beta_init = that mean field in real space plus
 Gaussian fluctuations of per-quadrature variance (max(n - |beta_init|^2, 0)
 + 1/2) / 2 (the reference's ReadFromSettings initial condition with a
 per-site beta_init and beta_init_sigma). The plain vacuum-initialised run
-stays the reference: a point whose warm-started steady density differs from the
-plain run's by more than `rerun_se` standard errors is replaced by its plain
-result (the rerun rule).
+stays the reference: a point whose warm-started steady density or g2 differs
+from the plain run's by more than `rerun_se` standard errors is replaced by
+its plain result (the rerun rule).
 
 Device work -- plain runs, field moments, MLP rows, training, inference,
 initial fields, warm runs -- goes through the C ABI (twmc_hbatch_*,
@@ -249,23 +249,43 @@ class WarmSweep:
     rerun: np.ndarray            # [P] bool: warm result rejected by the rerun rule
     n_final: np.ndarray          # [P] steady density after the rule
     g2_final: np.ndarray
+    init_s: float = 0.0          # wall time of the network inference and initial fields
+    warm_s: float = 0.0          # wall time of the warm-started runs
+    plain_s: float = 0.0         # wall time of the plain (judge) runs
+
+
+def rerun_mask(warm: SweepResult, plain: SweepResult, rerun_se=1.0) -> np.ndarray:
+    """The rerun rule: a warm-started point is replaced by its plain run when
+    its steady density n OR its g2 differs from the plain run's by more than
+    rerun_se combined standard errors, or when either is not finite."""
+    se_n = np.sqrt(warm.n_inf_se ** 2 + plain.n_inf_se ** 2)
+    se_g = np.sqrt(warm.g2_inf_se ** 2 + plain.g2_inf_se ** 2)
+    ok_n = np.abs(warm.n_inf - plain.n_inf) <= rerun_se * se_n        # False for NaN
+    ok_g = np.abs(warm.g2_inf - plain.g2_inf) <= rerun_se * se_g
+    return ~(ok_n & ok_g)
 
 
 def warm_sweep(ws: WarmStart, points, n_traj, t_end, dt=0.002, frame_period=0.5, seed0=1, rerun_se=1.0,
                tune=False):
-    """Warm-started sweep checked against plain runs: a point whose warm steady n
-    differs from the plain one by more than rerun_se combined standard
-    errors takes the plain result."""
+    """Warm-started sweep checked against plain runs: a point whose warm steady
+    n or g2 differs from the plain one by more than rerun_se combined standard
+    errors takes the plain result (rerun_mask)."""
+    import time
+    torch = _torch()
+    t0 = time.perf_counter()
     x = features(points)
     init = ws.initial_fields(x)
+    torch.cuda.synchronize()
+    t1 = time.perf_counter()
     warm = run_sweep(points, ws.nx, ws.ny, n_traj, t_end, dt, frame_period, init=init, seed0=seed0, tune=tune)
+    t2 = time.perf_counter()
     plain = run_sweep(points, ws.nx, ws.ny, n_traj, t_end, dt, frame_period, init=None, seed0=seed0 + 1000003,
                       tune=tune)
-    se = np.sqrt(warm.n_inf_se ** 2 + plain.n_inf_se ** 2)
-    rerun = ~(np.abs(warm.n_inf - plain.n_inf) <= rerun_se * se)   # non-finite warm results rerun too
+    t3 = time.perf_counter()
+    rerun = rerun_mask(warm, plain, rerun_se)
     n_final = np.where(rerun, plain.n_inf, warm.n_inf)
     g2_final = np.where(rerun, plain.g2_inf, warm.g2_inf)
-    return WarmSweep(warm, plain, rerun, n_final, g2_final)
+    return WarmSweep(warm, plain, rerun, n_final, g2_final, init_s=t1 - t0, warm_s=t2 - t1, plain_s=t3 - t2)
 
 
 def evaluate(L=32, n_train=1024, traj_train=256, t_train=20.0, n_test=64, traj_test=512, t_test=20.0,
@@ -292,6 +312,12 @@ def evaluate(L=32, n_train=1024, traj_train=256, t_train=20.0, n_test=64, traj_t
     se_n = np.sqrt(res.warm.n_inf_se ** 2 + res.plain.n_inf_se ** 2)
     se_g = np.sqrt(res.warm.g2_inf_se ** 2 + res.plain.g2_inf_se ** 2)
     ok = np.isfinite(se_g) & np.isfinite(res.warm.g2_inf)
+    # wall clock: the sweep's device time per unit of simulated time and
+    # point turns each point's time to steady state into seconds; a sweep
+    # that stops every point at its steady state costs the sum over points
+    per_point_s = res.plain.device_ms * 1e-3 / (len(test) * t_test)
+    wall_to_steady_plain = float(np.sum(res.plain.ttss) * per_point_s)
+    wall_to_steady_warm = float(np.sum(res.warm.ttss) * per_point_s) + res.init_s
     return {
         "workload": f"{L}x{L} PBC sweep, train {n_train} points x {traj_train} trajectories to t={t_train:g}, "
                     f"test {n_test} held-out points x {traj_test} trajectories to t={t_test:g}, dt=0.002, "
@@ -302,6 +328,21 @@ def evaluate(L=32, n_train=1024, traj_train=256, t_train=20.0, n_test=64, traj_t
         "g2_within_1se_frac": float(np.mean(np.abs(res.warm.g2_inf - res.plain.g2_inf)[ok] <= se_g[ok]))
         if ok.any() else None,
         "reruns": int(res.rerun.sum()), "test_points": n_test,
+        "rerun_rule": "warm point replaced by its plain run when n or g2 differs by > 1 combined SE",
+        "final_within_1se": "all points by construction (warm where it agrees, plain otherwise)",
+        "wall_s": {
+            "to_steady_state_plain": wall_to_steady_plain,
+            "to_steady_state_warm": wall_to_steady_warm,
+            "to_steady_state_speedup": wall_to_steady_plain / max(wall_to_steady_warm, 1e-9),
+            "definition": "sweep that stops each point at its time to steady state: sum over points of "
+                          "ttss x the sweep's measured device seconds per point and simulated time unit; warm "
+                          "adds the network inference and initial-field draws",
+            "training_data": t1 - t0, "fit": t2 - t1, "inference_and_init": res.init_s,
+            "warm_runs": res.warm_s, "plain_judge_runs": res.plain_s,
+            "warm_total_with_judge": (t1 - t0) + (t2 - t1) + res.init_s + res.warm_s + res.plain_s,
+            "plain_only": res.plain_s,
+            "note": "every warm point is judged by a full plain run here, so this sweep costs more than plain "
+                    "runs alone; the gain is the time to steady state of each point"},
         "train_s": t1 - t0, "train_site_updates_per_s": su / (t1 - t0), "fit_s": t2 - t1,
         "fit_steps": rep.steps, "mlp_launches": rep.launches, "final_loss": rep.losses[-1][1], "sweep_s": t3 - t2,
         "ttss_definition": "first save time with |n - n_inf| <= max(1 SE, 1e-3 n_inf), staying within 2x for "

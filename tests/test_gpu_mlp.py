@@ -191,7 +191,8 @@ def test_warm_start_cuts_time_to_steady_state(built_lib):
     the median time to steady state must drop at least 2.5x against the plain
     vacuum start, no warm run may diverge, and warm and plain steady
     densities must agree within 3 combined standard errors for >= 80% of the
-    points (the rerun rule replaces the others by the plain result)."""
+    points, and the rerun rule replaces every point whose n or g2 is off by
+    more than one combined standard error by its plain result."""
     from pincosimulator_gb300 import warmstart as wsm
 
     train = wsm.sample_points(512, seed=11)
@@ -208,3 +209,10 @@ def test_warm_start_cuts_time_to_steady_state(built_lib):
     se = np.sqrt(res.warm.n_inf_se ** 2 + res.plain.n_inf_se ** 2)
     assert np.mean(np.abs(res.warm.n_inf - res.plain.n_inf) <= 3 * se) >= 0.8
     assert np.array_equal(res.n_final[res.rerun], res.plain.n_inf[res.rerun])
+    # the rule judges n and g2: every kept warm point agrees with its plain run in both
+    keep = ~res.rerun
+    se_g = np.sqrt(res.warm.g2_inf_se ** 2 + res.plain.g2_inf_se ** 2)
+    assert np.all(np.abs(res.warm.n_inf - res.plain.n_inf)[keep] <= se[keep])
+    assert np.all(np.abs(res.warm.g2_inf - res.plain.g2_inf)[keep] <= se_g[keep])
+    assert np.array_equal(res.g2_final[res.rerun], res.plain.g2_inf[res.rerun])
+    assert np.array_equal(res.rerun, wsm.rerun_mask(res.warm, res.plain))
