@@ -163,28 +163,12 @@ def make_system(twmc, hop=None, precision=None):
                        hop=twmc.HOP_FFT if hop is None else hop, n_moment_blocks=32)
 
 
-def batch_points(seed=3):
-    """The heterogeneous-batch workload: 256 parameter points, each a chain of
-    32..1024 sites or an L x L lattice (L = 16..128), U ~ U[0.05, 0.5],
-    detuning ~ U[-2, 2], F ~ U[0, 3], J = gamma = 1, 512..4096 trajectories
-    (uniform in log), dt = 0.002, frames of 250 steps."""
-    import numpy as np
-    rng = np.random.default_rng(seed)
-    kinds = [(1, n) for n in (32, 64, 128, 256, 512, 1024)] + [(l, l) for l in (16, 32, 64, 128)]
-    pts = []
-    for _ in range(256):
-        nx, ny = kinds[rng.integers(len(kinds))]
-        pts.append(dict(nx=nx, ny=ny, U=rng.uniform(0.05, 0.5), omega=rng.uniform(-2, 2), F=rng.uniform(0, 3),
-                        dt=DT, n_traj=int(np.exp(rng.uniform(np.log(512), np.log(4096)))),
-                        seed0=int(rng.integers(1, 2 ** 31)), id0=1))
-    return pts
-
-
 def measure_batch(twmc, torch, sm_mhz=None, t_end=60.0):
     """The 256-point heterogeneous batch to its full t_end (120 frames of 250
     steps), autotuned step variants, every (point, trajectory group) a work
     item of the persistent queue kernels; device time of the whole run."""
     from collections import Counter
+    from pincosimulator_gb300.workloads import batch_points
     pts = batch_points()
     sites = sum(p["nx"] * p["ny"] * p["n_traj"] for p in pts)
     frames = int(round(t_end / (DT * FRAME_STEPS)))
@@ -311,16 +295,25 @@ def measure_observable_error(twmc, ntraj=256, t_end=T_END):
 
 
 def _cpu_cores():
-    """Host CPU description for the baseline record."""
-    model = ""
+    """Host CPU description for the baseline record: the model name, or on
+    Arm hosts (whose /proc/cpuinfo has none) the implementer and part ids."""
+    fields = {}
     try:
         for line in open("/proc/cpuinfo"):
-            k = line.split(":")[0].strip().lower()
-            if k in ("model name", "cpu model", "uarch") and not model:
-                model = line.split(":", 1)[1].strip()
+            if ":" in line:
+                k, v = line.split(":", 1)
+                fields.setdefault(k.strip().lower(), v.strip())
     except OSError:
         pass
+    model = fields.get("model name") or fields.get("cpu model") or ""
+    if not model and "cpu part" in fields:
+        model = f"{platform_machine()} (CPU implementer {fields.get('cpu implementer', '?')}, part {fields['cpu part']})"
     return os.cpu_count() or 1, model
+
+
+def platform_machine():
+    import platform
+    return platform.machine()
 
 
 def cpu_run(ntraj, steps, threads, build, noise):

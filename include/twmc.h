@@ -189,7 +189,8 @@ TWMC_API int twmc_batch_advance(twmc_handle* h, int64_t n_steps);
 /* Reduces the current batch state into FP64 moment blocks (asynchronous). */
 TWMC_API int twmc_batch_reduce(twmc_handle* h);
 /* Waits for the handle's stream; *kernel_ms = summed device time of the
- * trajectory-step launches since the last call (may be NULL). */
+ * trajectory-step launches since the last call (may be NULL), including those
+ * of twmc_run calls made since then. */
 TWMC_API int twmc_sync(twmc_handle* h, double* kernel_ms);
 /* Copies the batch state (n x n_sites complex128) and/or the last moment
  * blocks (n_moment_blocks x n_sites x 3) to host memory; NULL skips. */

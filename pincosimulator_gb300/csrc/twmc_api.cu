@@ -129,6 +129,7 @@ struct twmc_handle {
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_pending;
   std::vector<std::pair<cudaEvent_t, cudaEvent_t>> ev_free;
   int64_t launches = 0;
+  double carry_ms = 0.0;  // step-kernel device time of the last twmc_run, not yet reported
   double progress = 0.0;
   LaunchInfo last_info;
 };
@@ -843,7 +844,8 @@ int twmc_sync(twmc_handle* h, double* kernel_ms) {
   cudaSetDevice(h->device);
   cudaError_t e = cudaStreamSynchronize(h->stream);
   if (e != cudaSuccess) return cuda_fail(h, e, "cudaStreamSynchronize");
-  double ms = 0;
+  double ms = h->carry_ms;  // step launches of twmc_run calls since the last twmc_sync
+  h->carry_ms = 0.0;
   for (auto& ev : h->ev_pending) {
     float x = 0;
     if (cudaEventElapsedTime(&x, ev.first, ev.second) == cudaSuccess) ms += x;
@@ -889,6 +891,8 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
     cudaSetDevice(h->device);
     h->err.clear();
     h->progress = 0.0;
+    double run_ms = h->carry_ms;  // step time not yet reported to the caller
+    h->carry_ms = 0.0;
     const int64_t N = h->nsites;
     // group tasks by (t_start, t_end, store_initial, ic_kind)
     std::map<std::tuple<double, double, int, int>, std::vector<size_t>> groups;
@@ -1125,12 +1129,14 @@ int twmc_run(twmc_handle* h, const twmc_task_desc* tasks, size_t n, twmc_outputs
         if (out && out->t_final) out->t_final[idx[i]] = s.t_final;
         if (out && out->frames_written) out->frames_written[idx[i]] = s.frames_written;
       }
-      double ms;
+      double ms = 0.0;
       rc = twmc_sync(h, &ms);
       if (rc) return rc;
+      run_ms += ms;
     }
     h->progress = 1.0;
     h->noise_set = false;
+    h->carry_ms = run_ms;  // reported by the caller's next twmc_sync
     return TWMC_OK;
   } catch (const std::bad_alloc&) {
     return fail(h, TWMC_ERR_NOMEM, "host allocation failed");

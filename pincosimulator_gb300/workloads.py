@@ -9,6 +9,9 @@
   F=1.5, beta_init_sigma=0.5, dt=0.005, a frame every 100 steps: the
   configuration of the reference's own CPU runs (1000 trajectories to
   t = 50 there). Timed through ``twmc_run`` with every frame saved.
+* ``batch256``  -- the 256-point heterogeneous batch (chains of 32..1024
+  sites and 16..128 square lattices, 512..4096 trajectories per point,
+  autotuned step variants), timed with CUDA events.
 * ``lieb768``   -- the 1-D Lieb lattice of 256 cells (768 sites), PBC,
   J_AB=J_BC=1, gamma=1, U=0.27 with uniform disorder of amplitude 0.06, and a
   drive F(t) on the B sites ramping from 0 to 2.5 over t in [0, 40] in
@@ -55,6 +58,36 @@ def chain64(hop=twmc.HOP_FFT):
                        beta_init=0.0, beta_init_sigma=0.5, hop=hop)
 
 
+def batch_points(seed=3, traj_scale=1.0):
+    """The heterogeneous-batch workload: 256 parameter points, each a chain of
+    32..1024 sites or an L x L lattice (L = 16..128), U ~ U[0.05, 0.5],
+    detuning ~ U[-2, 2], F ~ U[0, 3], J = gamma = 1, 512..4096 trajectories
+    (uniform in log; times traj_scale, at least 1), dt = 0.002."""
+    rng = np.random.default_rng(seed)
+    kinds = [(1, n) for n in (32, 64, 128, 256, 512, 1024)] + [(l, l) for l in (16, 32, 64, 128)]
+    pts = []
+    for _ in range(256):
+        nx, ny = kinds[rng.integers(len(kinds))]
+        u, om, f = rng.uniform(0.05, 0.5), rng.uniform(-2, 2), rng.uniform(0, 3)
+        nt = int(np.exp(rng.uniform(np.log(512), np.log(4096))))
+        pts.append(dict(nx=nx, ny=ny, U=u, omega=om, F=f, dt=DT, n_traj=max(1, int(nt * traj_scale)),
+                        seed0=int(rng.integers(1, 2 ** 31)), id0=1))
+    return pts
+
+
+def time_hbatch(points, frames, tune=True):
+    """Device time (CUDA events) of `frames` frames of a heterogeneous batch
+    after one untimed frame; returns (seconds, total site-trajectories, plans)."""
+    hb = twmc.HBatch(points, FRAME_STEPS, tune=tune)
+    plans = [hb.plan(i) for i in range(len(points))]
+    hb.run(1)
+    hb.sync()
+    hb.run(frames)
+    ms = hb.sync()
+    hb.close()
+    return ms / 1e3, sum(p["nx"] * p["ny"] * p["n_traj"] for p in points), plans
+
+
 def time_run(sysd, ntraj, frames, save=False):
     """Wall time of one twmc_run call of `frames` frames (after an untimed
     call); with `save`, every frame and the final field are returned."""
@@ -84,11 +117,18 @@ def time_batch(sysd, ntraj, frames):
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
-    ap.add_argument("workload", choices=["square64", "square128", "lieb768", "chain64"])
+    ap.add_argument("workload", choices=["square64", "square128", "lieb768", "chain64", "batch256"])
+    ap.add_argument("--traj-scale", type=float, default=1.0, help="batch256: trajectories per point x this")
     ap.add_argument("--ntraj", type=int, default=2048)
     ap.add_argument("--frames", type=int, default=1)
     ap.add_argument("--hop", choices=["fft", "stencil"], default="stencil")
     args = ap.parse_args(argv)
+    if args.workload == "batch256":
+        el, sites, plans = time_hbatch(batch_points(traj_scale=args.traj_scale), args.frames)
+        print(json.dumps({"workload": "batch256", "traj_scale": args.traj_scale, "frames": args.frames,
+                          "seconds": el, "site_updates_per_s": sites * FRAME_STEPS * args.frames / el,
+                          "variants": sorted(set(p.split("<")[1].split(" ")[0] for p in plans))}), flush=True)
+        return
     if args.workload == "lieb768":
         sysd = lieb()
         el, finite = time_run(sysd, args.ntraj, args.frames)

@@ -5,7 +5,8 @@ SampleData/F_t.dat of the PincoSimulator project (the only fixtures it ships;
 they pin input parsing, not results). test-lieb.ini names matrix files
 _E.dat, _F.dat and _U.dat that the project does not ship; this script writes
 small synthetic ones (24 cells x 3 sites, column-major values) so the file
-resolves. Run once where the reference is mounted:
+resolves. Run once where the reference is mounted, with its root as the
+argument or in $PINCO_REFERENCE_ROOT:
 
     python tests/golden/make_fixtures.py /path/to/PincoSimulator
 """
@@ -33,4 +34,7 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("PINCO_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: make_fixtures.py <PincoSimulator root> (or set PINCO_REFERENCE_ROOT)")
+    main(root)
