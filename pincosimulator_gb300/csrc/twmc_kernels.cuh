@@ -140,6 +140,62 @@ template <> struct Wiener<double> {
 };
 
 // ------------------------------------------------------------------------
+// compile-time twiddles: (cos, sin)(2 pi k / M) in double by an exact octant
+// reduction of the integer k and Taylor series on |x| <= pi / 4
+// ------------------------------------------------------------------------
+struct CosSin { double c, s; };
+constexpr double kPiD = 3.14159265358979323846264338327950288;
+constexpr double taylor_sin(double x) {
+  double x2 = x * x, term = x, sum = x;
+  for (int n = 1; n < 12; ++n) { term *= -x2 / double((2 * n) * (2 * n + 1)); sum += term; }
+  return sum;
+}
+constexpr double taylor_cos(double x) {
+  double x2 = x * x, term = 1.0, sum = 1.0;
+  for (int n = 1; n < 12; ++n) { term *= -x2 / double((2 * n - 1) * (2 * n)); sum += term; }
+  return sum;
+}
+constexpr CosSin cossin2pi(int k, int M) {
+  k %= M;
+  if (k < 0) k += M;
+  if (2 * k > M) {  // (pi, 2 pi): the conjugate of 2 pi (M - k) / M
+    const CosSin r = cossin2pi(M - k, M);
+    return CosSin{r.c, -r.s};
+  }
+  if (4 * k > M) {  // (pi / 2, pi]: pi - theta
+    const CosSin r = cossin2pi(M - 2 * k, 2 * M);  // angle pi - 2 pi k / M = 2 pi (M - 2k) / (2M)
+    return CosSin{-r.c, r.s};
+  }
+  if (8 * k > M) {  // (pi / 4, pi / 2]: pi / 2 - theta
+    const double x = kPiD * double(M - 4 * k) / double(2 * M);
+    return CosSin{taylor_sin(x), taylor_cos(x)};
+  }
+  const double x = 2.0 * kPiD * double(k) / double(M);
+  return CosSin{taylor_cos(x), taylor_sin(x)};
+}
+
+// x * W_M^E (W = e^{-2 pi i / M}) or x * conj(W_M^E) for a compile-time E:
+// quarter turns as swaps and sign changes, other twiddles as immediates.
+template <typename T, int M, int E, bool CONJ>
+__device__ __forceinline__ T cmul_tw(T x) {
+  using R = decltype(T::x);
+  constexpr int e = ((E % M) + M) % M;
+  if constexpr (e == 0) {
+    return x;
+  } else if constexpr (2 * e == M) {
+    return cmake<T>(-x.x, -x.y);
+  } else if constexpr (4 * e == M) {  // W = -i
+    return CONJ ? cmake<T>(-x.y, x.x) : cmake<T>(x.y, -x.x);
+  } else if constexpr (4 * e == 3 * M) {  // W = +i
+    return CONJ ? cmake<T>(x.y, -x.x) : cmake<T>(-x.y, x.x);
+  } else {
+    constexpr CosSin w = cossin2pi(e, M);
+    const T wv = cmake<T>(R(w.c), R(-w.s));
+    return CONJ ? cmulc(x, wv) : cmul(x, wv);
+  }
+}
+
+// ------------------------------------------------------------------------
 // compile-time plan helpers (P = generated Plan_bx_by)
 // ------------------------------------------------------------------------
 template <class P> struct PlanInfo {
@@ -218,8 +274,12 @@ __device__ __forceinline__ void fft_stage(T (&x)[PlanInfo<P>::E], const T* __res
       constexpr int s1 = s0 | (1 << j0), s2 = s0 | (1 << j1), s3 = s0 | (1 << j0) | (1 << j1);
       constexpr int low_r = int((uint32_t(I::pos_reg(K, s0)) & lowmask) >> lo);
       constexpr bool trivial = !thr_low && low_r == 0;
+      // twiddles W_M^{j e1}: from the table when thread bits enter the
+      // exponent, compile-time constants (immediates, exact quarter turns)
+      // when only register bits do
+      constexpr int MM = 1 << m, ec = low_r << sh;
       T w1, w2, w3;
-      if constexpr (!trivial) {
+      if constexpr (thr_low) {
         const int e1 = (low_r + low_t) << sh;
         w1 = tw[e1];
         w2 = tw[2 * e1];
@@ -231,18 +291,26 @@ __device__ __forceinline__ void fft_stage(T (&x)[PlanInfo<P>::E], const T* __res
         T y0 = cadd(A, B), y1 = csub(A, B);
         T y2 = cmake<T>(C.x + D.y, C.y - D.x);  // C - iD
         T y3 = cmake<T>(C.x - D.y, C.y + D.x);  // C + iD
-        if constexpr (!trivial) {
+        if constexpr (thr_low) {
           y1 = cmul(y1, w2);
           y2 = cmul(y2, w1);
           y3 = cmul(y3, w3);
+        } else if constexpr (!trivial) {
+          y1 = cmul_tw<T, MM, 2 * ec, false>(y1);
+          y2 = cmul_tw<T, MM, ec, false>(y2);
+          y3 = cmul_tw<T, MM, 3 * ec, false>(y3);
         }
         x[s0] = y0; x[s1] = y1; x[s2] = y2; x[s3] = y3;
       } else {
         T u = x[s1], p = x[s2], q = x[s3];
-        if constexpr (!trivial) {
+        if constexpr (thr_low) {
           u = cmulc(u, w2);
           p = cmulc(p, w1);
           q = cmulc(q, w3);
+        } else if constexpr (!trivial) {
+          u = cmul_tw<T, MM, 2 * ec, true>(u);
+          p = cmul_tw<T, MM, ec, true>(p);
+          q = cmul_tw<T, MM, 3 * ec, true>(q);
         }
         const T A = cadd(x[s0], u), B = csub(x[s0], u);
         const T C = cadd(p, q);
@@ -260,15 +328,18 @@ __device__ __forceinline__ void fft_stage(T (&x)[PlanInfo<P>::E], const T* __res
       constexpr int s1 = s0 | (1 << j0);
       constexpr int low_r = int((uint32_t(I::pos_reg(K, s0)) & lowmask) >> lo);
       constexpr bool trivial = !thr_low && low_r == 0;
+      constexpr int MM = 1 << m, ec = low_r << sh;
       T w;
-      if constexpr (!trivial) w = tw[(low_r + low_t) << sh];
+      if constexpr (thr_low) w = tw[(low_r + low_t) << sh];
       if constexpr (!INV) {
         T y0 = cadd(x[s0], x[s1]), y1 = csub(x[s0], x[s1]);
-        if constexpr (!trivial) y1 = cmul(y1, w);
+        if constexpr (thr_low) y1 = cmul(y1, w);
+        else if constexpr (!trivial) y1 = cmul_tw<T, MM, ec, false>(y1);
         x[s0] = y0; x[s1] = y1;
       } else {
         T u = x[s1];
-        if constexpr (!trivial) u = cmulc(u, w);
+        if constexpr (thr_low) u = cmulc(u, w);
+        else if constexpr (!trivial) u = cmul_tw<T, MM, ec, true>(u);
         const T y0 = x[s0];
         x[s0] = cadd(y0, u); x[s1] = csub(y0, u);
       }
