@@ -245,15 +245,69 @@ template <class P> struct PlanInfo {
   }
 };
 
+// Register slots of the twiddles that depend on thread bits (stages whose
+// exponent mixes thread and register bits): one set per distinct register
+// part of the exponent, three values (W^e, W^2e, W^3e) for a radix-4 stage
+// and one for radix-2. The set is the same for the forward and the inverse
+// transform (conjugated there), and loop-invariant per thread, so a kernel
+// with registers to spare loads it once per launch.
+template <class P> struct TwSlots {
+  using I = PlanInfo<P>;
+  static constexpr uint32_t lowmask(int K, int SI) {
+    return ((1u << P::st[K][SI][1]) - 1u) << P::lo[P::st[K][SI][0]];
+  }
+  static constexpr bool thr_low(int K, int SI) { return (I::thr_mask(K) & lowmask(K, SI)) != 0u; }
+  static constexpr int ngroups(int K, int SI) { return P::st[K][SI][2] == 2 ? I::E / 4 : I::E / 2; }
+  static constexpr int low_r(int K, int SI, int Q) {
+    const int dim = P::st[K][SI][0], t = P::st[K][SI][1], lo = P::lo[dim];
+    const int j0 = I::slot_bit(K, lo + t);
+    const int j1 = P::st[K][SI][2] == 2 ? I::slot_bit(K, lo + t + 1) : -1;
+    const int s0 = I::insert0(Q, j0, j1);
+    return int((uint32_t(I::pos_reg(K, s0)) & lowmask(K, SI)) >> lo);
+  }
+  // index of group Q's register part among the distinct ones of its stage
+  static constexpr int distinct(int K, int SI, int Q) {
+    int d = 0;
+    for (int q = 0; q < Q; ++q) {
+      bool seen = false;
+      for (int r = 0; r < q; ++r) seen = seen || low_r(K, SI, r) == low_r(K, SI, q);
+      if (seen) continue;
+      if (low_r(K, SI, q) == low_r(K, SI, Q)) return d;
+      ++d;
+    }
+    return d;
+  }
+  static constexpr int ndistinct(int K, int SI) {
+    int d = 0;
+    for (int q = 0; q < ngroups(K, SI); ++q) {
+      bool seen = false;
+      for (int r = 0; r < q; ++r) seen = seen || low_r(K, SI, r) == low_r(K, SI, q);
+      if (!seen) ++d;
+    }
+    return d;
+  }
+  static constexpr int per(int K, int SI) { return P::st[K][SI][2] == 2 ? 3 : 1; }
+  static constexpr int base(int K, int SI) {
+    int b = 0;
+    for (int k = 0; k < P::npass; ++k)
+      for (int si = 0; si < P::nst[k]; ++si) {
+        if (k == K && si == SI) return b;
+        if (thr_low(k, si)) b += ndistinct(k, si) * per(k, si);
+      }
+    return b;
+  }
+  static constexpr int total() { return base(P::npass, 0); }
+};
+
 // Padded position of the CTA-flat element index: one pad slot after every 16
 // elements. For indices with disjoint bits pad(a | b) = pad(a) + pad(b), so
 // the thread part is a register and the register-slot part an immediate.
 __host__ __device__ constexpr int pad16(int p) { return p + (p >> 4); }
 
 // One DIF stage (forward) or its adjoint (inverse) of pass K, stage SI.
-template <class P, int K, int SI, bool INV, typename T>
+template <class P, int K, int SI, bool INV, bool HT, typename T>
 __device__ __forceinline__ void fft_stage(T (&x)[PlanInfo<P>::E], const T* __restrict__ tw0,
-                                          const T* __restrict__ tw1, int pos_thr) {
+                                          const T* __restrict__ tw1, int pos_thr, const T* twr) {
   using I = PlanInfo<P>;
   constexpr int dim = P::st[K][SI][0];
   constexpr int t = P::st[K][SI][1];
@@ -273,13 +327,18 @@ __device__ __forceinline__ void fft_stage(T (&x)[PlanInfo<P>::E], const T* __res
       constexpr int s0 = I::insert0(decltype(Q)::value, j0, j1);
       constexpr int s1 = s0 | (1 << j0), s2 = s0 | (1 << j1), s3 = s0 | (1 << j0) | (1 << j1);
       constexpr int low_r = int((uint32_t(I::pos_reg(K, s0)) & lowmask) >> lo);
-      constexpr bool trivial = !thr_low && low_r == 0;
+      [[maybe_unused]] constexpr bool trivial = !thr_low && low_r == 0;
       // twiddles W_M^{j e1}: from the table when thread bits enter the
       // exponent, compile-time constants (immediates, exact quarter turns)
       // when only register bits do
-      constexpr int MM = 1 << m, ec = low_r << sh;
-      T w1, w2, w3;
-      if constexpr (thr_low) {
+      [[maybe_unused]] constexpr int MM = 1 << m, ec = low_r << sh;
+      [[maybe_unused]] T w1, w2, w3;
+      if constexpr (thr_low && HT) {  // the launch-invariant set held in registers
+        constexpr int slot = TwSlots<P>::base(K, SI) + 3 * TwSlots<P>::distinct(K, SI, decltype(Q)::value);
+        w1 = twr[slot];
+        w2 = twr[slot + 1];
+        w3 = twr[slot + 2];
+      } else if constexpr (thr_low) {
         const int e1 = (low_r + low_t) << sh;
         w1 = tw[e1];
         w2 = tw[2 * e1];
@@ -327,10 +386,11 @@ __device__ __forceinline__ void fft_stage(T (&x)[PlanInfo<P>::E], const T* __res
       constexpr int s0 = I::insert0(decltype(Q)::value, j0, -1);
       constexpr int s1 = s0 | (1 << j0);
       constexpr int low_r = int((uint32_t(I::pos_reg(K, s0)) & lowmask) >> lo);
-      constexpr bool trivial = !thr_low && low_r == 0;
-      constexpr int MM = 1 << m, ec = low_r << sh;
-      T w;
-      if constexpr (thr_low) w = tw[(low_r + low_t) << sh];
+      [[maybe_unused]] constexpr bool trivial = !thr_low && low_r == 0;
+      [[maybe_unused]] constexpr int MM = 1 << m, ec = low_r << sh;
+      [[maybe_unused]] T w;
+      if constexpr (thr_low && HT) w = twr[TwSlots<P>::base(K, SI) + TwSlots<P>::distinct(K, SI, decltype(Q)::value)];
+      else if constexpr (thr_low) w = tw[(low_r + low_t) << sh];
       if constexpr (!INV) {
         T y0 = cadd(x[s0], x[s1]), y1 = csub(x[s0], x[s1]);
         if constexpr (thr_low) y1 = cmul(y1, w);
@@ -347,12 +407,49 @@ __device__ __forceinline__ void fft_stage(T (&x)[PlanInfo<P>::E], const T* __res
   }
 }
 
-template <class P, int K, bool INV, typename T>
-__device__ __forceinline__ void fft_pass(T (&x)[PlanInfo<P>::E], const T* tw0, const T* tw1, int pos_thr) {
+template <class P, int K, bool INV, bool HT = false, typename T>
+__device__ __forceinline__ void fft_pass(T (&x)[PlanInfo<P>::E], const T* tw0, const T* tw1, int pos_thr,
+                                         const T* twr = nullptr) {
   constexpr int ns = P::nst[K];
   static_for<ns>([&](auto S) {
     constexpr int si = INV ? (ns - 1 - decltype(S)::value) : decltype(S)::value;
-    fft_stage<P, K, si, INV>(x, tw0, tw1, pos_thr);
+    fft_stage<P, K, si, INV, HT>(x, tw0, tw1, pos_thr, twr);
+  });
+}
+
+// The twiddle register set of TwSlots for this thread (table loads, once).
+template <class P, typename T>
+__device__ __forceinline__ void load_twiddle_set(T* twr, const T* tw0, const T* tw1, const int* pos_thr) {
+  using S = TwSlots<P>;
+  static_for<P::npass>([&](auto KK) {
+    constexpr int K = decltype(KK)::value;
+    static_for<P::nst[K]>([&](auto SS) {
+      constexpr int SI = decltype(SS)::value;
+      if constexpr (S::thr_low(K, SI)) {
+        constexpr int dim = P::st[K][SI][0], t = P::st[K][SI][1], lo = P::lo[dim], m = P::m[dim];
+        constexpr int sh = P::st[K][SI][2] == 2 ? m - t - 2 : m - t - 1;
+        const T* tw = dim ? tw1 : tw0;
+        const int low_t = int((uint32_t(pos_thr[K]) & S::lowmask(K, SI)) >> lo);
+        static_for<S::ngroups(K, SI)>([&](auto QQ) {
+          constexpr int Q = decltype(QQ)::value;
+          constexpr int d = S::distinct(K, SI, Q);
+          constexpr bool first = [] {
+            for (int q = 0; q < Q; ++q) if (S::distinct(K, SI, q) == S::distinct(K, SI, Q)) return false;
+            return true;
+          }();
+          if constexpr (first) {
+            const int e1 = (S::low_r(K, SI, Q) + low_t) << sh;
+            if constexpr (S::per(K, SI) == 3) {
+              twr[S::base(K, SI) + 3 * d] = tw[e1];
+              twr[S::base(K, SI) + 3 * d + 1] = tw[2 * e1];
+              twr[S::base(K, SI) + 3 * d + 2] = tw[3 * e1];
+            } else {
+              twr[S::base(K, SI) + d] = tw[e1];
+            }
+          }
+        });
+      }
+    });
   });
 }
 
@@ -487,6 +584,15 @@ struct SquareGroup {
     const T* __restrict__ g_iF = has_iF ? reinterpret_cast<const T*>(a.iF) + tr * a.par_stride : nullptr;
     const uint32_t seed = a.seeds[tr], id = a.ids[tr];
     const T* noise_tr = reinterpret_cast<const T*>(a.noise) + tr * a.noise_traj_stride;
+    // single-system FP32 kernel (no register cap), chains of 1024 sites and
+    // more: the thread-dependent twiddles in registers for the whole launch.
+    // Their per-step table loads are strided across threads there (bank
+    // conflicts on a 3072-entry table); measured on GB300: 1x4096 0.95e11 ->
+    // 1.74e11 site-updates/s, 1x1024 1.90e11 -> 2.05e11, while 64x64 (-11 %),
+    // 32x32 (-3 %) and 1x256 (-5 %) lost to the extra register pressure.
+    constexpr bool HT = REG_SMALL && sizeof(R) == 4 && P::bx == 0 && P::nbits >= 10 && TwSlots<P>::total() > 0;
+    T twr[HT ? TwSlots<P>::total() : 1];
+    if constexpr (HT) load_twiddle_set<P>(twr, tw0, tw1, pos_thr);
 
     for (int64_t step = 0; step < a.nsteps; ++step) {
       T x[E];
@@ -498,7 +604,7 @@ struct SquareGroup {
           fft_exchange<P, k - 1, k, Cfg::SYNC_WARP>(x, s_x + buf * Cfg::XSZ, xbase[k - 1], xbase[k]);
           buf ^= 1;
         }
-        fft_pass<P, k, false>(x, tw0, tw1, pos_thr[k]);
+        fft_pass<P, k, false, HT>(x, tw0, tw1, pos_thr[k], twr);
       });
       // k-space multiply by -i 2J (cos kx + cos ky) / N
       static_for<E>([&](auto S) {
@@ -511,7 +617,7 @@ struct SquareGroup {
       // inverse FFT (adjoint passes in reverse order)
       static_for<NP>([&](auto KK) {
         constexpr int k = LAST - decltype(KK)::value;
-        fft_pass<P, k, true>(x, tw0, tw1, pos_thr[k]);
+        fft_pass<P, k, true, HT>(x, tw0, tw1, pos_thr[k], twr);
         if constexpr (k > 0) {
           fft_exchange<P, k, k - 1, Cfg::SYNC_WARP>(x, s_x + buf * Cfg::XSZ, xbase[k], xbase[k - 1]);
           buf ^= 1;
