@@ -26,6 +26,15 @@ template <> __device__ __forceinline__ float2 csub<float2>(float2 a, float2 b) {
 template <typename T> __device__ __forceinline__ T cmul(T a, T b) { return cmake<T>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); }
 // a * conj(b)
 template <typename T> __device__ __forceinline__ T cmulc(T a, T b) { return cmake<T>(a.x * b.x + a.y * b.y, a.y * b.x - a.x * b.y); }
+// acc + y * conj(w) as four multiply-adds (one rounding per component step)
+template <typename T> __device__ __forceinline__ T cmlac(T acc, T y, T w) {
+  return cmake<T>(fma(y.x, w.x, fma(y.y, w.y, acc.x)), fma(y.y, w.x, fma(-y.x, w.y, acc.y)));
+}
+// 2 a - s: the difference a - u of a butterfly whose sum s = a + u is known
+template <typename T> __device__ __forceinline__ T ctwice_minus(T a, T s) {
+  using R = decltype(T::x);
+  return cmake<T>(fma(R(2), a.x, -s.x), fma(R(2), a.y, -s.y));
+}
 // -i * a and +i * a
 template <typename T> __device__ __forceinline__ T cmul_mi(T a) { return cmake<T>(a.y, -a.x); }
 template <typename T> __device__ __forceinline__ T cmul_pi(T a) { return cmake<T>(-a.y, a.x); }

@@ -107,15 +107,23 @@ __device__ __forceinline__ T local_update(T b, T h, T rsl, T iU, T iF, R dt, R d
 // FP32 form of the same update with dt folded in: b' = (A + B |b|^2) b + h' +
 // F' + dt4 xi, A = 1 + dt (rsl - iU), B = dt iU, F' = dt iF, h' = dt h (the
 // k-space table carries dt). Equal to local_update up to FP32 rounding.
-template <typename T, typename R>
+// MADD: the additive terms summed first and the product c b accumulated onto
+// them by four multiply-adds (eight FMA-pipe operations per site for the
+// product and the sums instead of ten).
+template <bool MADD = false, typename T, typename R>
 __device__ __forceinline__ T local_update_fused(T b, T hdt, T rsl, T iU, T iF, R dt, R dt4, T xi) {
   const T A = cmake<T>(R(1) + dt * (rsl.x - iU.x), dt * (rsl.y - iU.y));
   const T B = cmake<T>(dt * iU.x, dt * iU.y);
   const R ab2 = b.x * b.x + b.y * b.y;
   const T c = cmake<T>(A.x + B.x * ab2, A.y + B.y * ab2);
-  T nb = cmul(c, b);
-  nb = cmake<T>(nb.x + hdt.x + dt * iF.x, nb.y + hdt.y + dt * iF.y);
-  return cmake<T>(nb.x + dt4 * xi.x, nb.y + dt4 * xi.y);
+  if constexpr (MADD) {
+    const T w = cmake<T>(hdt.x + (dt * iF.x + dt4 * xi.x), hdt.y + (dt * iF.y + dt4 * xi.y));
+    return cmake<T>(fma(c.x, b.x, fma(-c.y, b.y, w.x)), fma(c.x, b.y, fma(c.y, b.x, w.y)));
+  } else {
+    T nb = cmul(c, b);
+    nb = cmake<T>(nb.x + hdt.x + dt * iF.x, nb.y + hdt.y + dt * iF.y);
+    return cmake<T>(nb.x + dt4 * xi.x, nb.y + dt4 * xi.y);
+  }
 }
 
 // Wiener term of one Philox word pair in the form the updates add it: FP32
@@ -193,6 +201,21 @@ __device__ __forceinline__ T cmul_tw(T x) {
     const T wv = cmake<T>(R(w.c), R(-w.s));
     return CONJ ? cmulc(x, wv) : cmul(x, wv);
   }
+}
+
+// Whether W_M^E is a general twiddle (not 1, -1 or a quarter turn).
+template <int M, int E>
+constexpr bool tw_general() {
+  constexpr int e = ((E % M) + M) % M;
+  return e != 0 && 2 * e != M && 4 * e != M && 4 * e != 3 * M;
+}
+// acc + y * W_M^E (or conj(W_M^E)) for a general compile-time twiddle: four
+// multiply-adds with immediates.
+template <typename T, int M, int E, bool CONJ>
+__device__ __forceinline__ T cmla_tw(T acc, T y) {
+  using R = decltype(T::x);
+  constexpr CosSin w = cossin2pi(((E % M) + M) % M, M);
+  return CONJ ? cmlac(acc, y, cmake<T>(R(w.c), R(-w.s))) : cmlac(acc, y, cmake<T>(R(w.c), R(w.s)));
 }
 
 // ------------------------------------------------------------------------
@@ -360,6 +383,41 @@ __device__ __forceinline__ void fft_stage(T (&x)[PlanInfo<P>::E], const T* __res
           y3 = cmul_tw<T, MM, 3 * ec, false>(y3);
         }
         x[s0] = y0; x[s1] = y1; x[s2] = y2; x[s3] = y3;
+      } else if constexpr (sizeof(decltype(T::x)) == 4) {
+        // FP32: each general twiddle product is accumulated onto its partner
+        // by multiply-adds (A = y0 + u, C = p + q) and the differences taken
+        // as 2 y0 - A, 2 p - C: 24 FMA-pipe operations per butterfly with
+        // three general twiddles instead of 28 (measured on GB300: 64x64
+        // 2.14e11 -> 2.19e11, 32x32 2.23e11 -> 2.30e11 site-updates/s)
+        const T y0 = x[s0];
+        T A, B, C, pq, p;
+        if constexpr (thr_low) {
+          A = cmlac(y0, x[s1], w2);
+          B = ctwice_minus(y0, A);
+          p = cmulc(x[s2], w1);
+          C = cmlac(p, x[s3], w3);
+          pq = ctwice_minus(p, C);
+        } else {
+          if constexpr (!trivial && tw_general<MM, 2 * ec>()) {
+            A = cmla_tw<T, MM, 2 * ec, true>(y0, x[s1]);
+            B = ctwice_minus(y0, A);
+          } else {
+            const T u = trivial ? x[s1] : cmul_tw<T, MM, 2 * ec, true>(x[s1]);
+            A = cadd(y0, u);
+            B = csub(y0, u);
+          }
+          p = trivial ? x[s2] : cmul_tw<T, MM, ec, true>(x[s2]);
+          if constexpr (!trivial && tw_general<MM, 3 * ec>()) {
+            C = cmla_tw<T, MM, 3 * ec, true>(p, x[s3]);
+            pq = ctwice_minus(p, C);
+          } else {
+            const T q = trivial ? x[s3] : cmul_tw<T, MM, 3 * ec, true>(x[s3]);
+            C = cadd(p, q);
+            pq = csub(p, q);
+          }
+        }
+        const T D = cmake<T>(-pq.y, pq.x);  // i (p - q)
+        x[s0] = cadd(A, C); x[s2] = csub(A, C); x[s1] = cadd(B, D); x[s3] = csub(B, D);
       } else {
         T u = x[s1], p = x[s2], q = x[s3];
         if constexpr (thr_low) {
@@ -396,6 +454,12 @@ __device__ __forceinline__ void fft_stage(T (&x)[PlanInfo<P>::E], const T* __res
         if constexpr (thr_low) y1 = cmul(y1, w);
         else if constexpr (!trivial) y1 = cmul_tw<T, MM, ec, false>(y1);
         x[s0] = y0; x[s1] = y1;
+      } else if constexpr (sizeof(decltype(T::x)) == 4 && (thr_low || (!trivial && tw_general<MM, ec>()))) {
+        const T y0 = x[s0];
+        T A;
+        if constexpr (thr_low) A = cmlac(y0, x[s1], w);
+        else A = cmla_tw<T, MM, ec, true>(y0, x[s1]);
+        x[s0] = A; x[s1] = ctwice_minus(y0, A);
       } else {
         T u = x[s1];
         if constexpr (thr_low) u = cmulc(u, w);
@@ -594,9 +658,21 @@ struct SquareGroup {
     T twr[HT ? TwSlots<P>::total() : 1];
     if constexpr (HT) load_twiddle_set<P>(twr, tw0, tw1, pos_thr);
 
+    // CARRY: x holds the state at the top of every step, loaded once and then
+    // carried from the local update (which also stores it to the slices),
+    // instead of reloaded from the slices every step; measured on GB300:
+    // 64x64 0.4 % faster, while the chains with their twiddles in registers
+    // (HT) lost 6 % to the longer register lifetimes. Those chains take the
+    // multiply-add form of the local update (local_update_fused<true>):
+    // 1x4096 1.77e11 -> 1.79e11, 1x1024 2.05e11 -> 2.09e11 site-updates/s,
+    // while 64x64 (2.19e11 -> 2.14e11), 32x32 and 1x256 were faster
+    // without it.
+    constexpr bool CARRY = !HT;
+    T x[E];
+    static_for<E>([&](auto S) { x[decltype(S)::value] = bget(S); });
     for (int64_t step = 0; step < a.nsteps; ++step) {
-      T x[E];
-      static_for<E>([&](auto S) { x[decltype(S)::value] = bget(S); });
+      const uint32_t gstep = a.step0 + uint32_t(step);
+      if constexpr (!CARRY) static_for<E>([&](auto S) { x[decltype(S)::value] = bget(S); });
       // forward FFT
       static_for<NP>([&](auto KK) {
         constexpr int k = decltype(KK)::value;
@@ -624,7 +700,6 @@ struct SquareGroup {
         }
       });
       // noise + local update (pass-0 layout: slot bit e-1 is the top site bit)
-      const uint32_t gstep = a.step0 + uint32_t(step);
       static_for<E / 2>([&](auto Q) {
         constexpr int s_lo = decltype(Q)::value;          // top slot bit clear
         constexpr int s_hi = s_lo | (E / 2);
@@ -649,12 +724,19 @@ struct SquareGroup {
         }
         constexpr std::integral_constant<int, s_lo> SL{};
         constexpr std::integral_constant<int, s_hi> SH{};
+        T n_lo, n_hi;
         if constexpr (sizeof(R) == 4) {  // dt is folded into the k-space table
-          bset(SL, local_update_fused(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo));
-          bset(SH, local_update_fused(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi));
+          n_lo = local_update_fused<HT>(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo);
+          n_hi = local_update_fused<HT>(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi);
         } else {
-          bset(SL, local_update(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo));
-          bset(SH, local_update(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi));
+          n_lo = local_update(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo);
+          n_hi = local_update(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi);
+        }
+        bset(SL, n_lo);
+        bset(SH, n_hi);
+        if constexpr (CARRY) {
+          x[s_lo] = n_lo;
+          x[s_hi] = n_hi;
         }
       });
     }
