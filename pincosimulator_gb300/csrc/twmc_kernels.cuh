@@ -204,10 +204,13 @@ __device__ __forceinline__ T cmul_tw(T x) {
 }
 
 // Whether W_M^E is a general twiddle (not 1, -1 or a quarter turn).
+constexpr bool tw_is_general(int M, int E) {
+  const int e = ((E % M) + M) % M;
+  return e != 0 && 2 * e != M && 4 * e != M && 4 * e != 3 * M;
+}
 template <int M, int E>
 constexpr bool tw_general() {
-  constexpr int e = ((E % M) + M) % M;
-  return e != 0 && 2 * e != M && 4 * e != M && 4 * e != 3 * M;
+  return tw_is_general(M, E);
 }
 // acc + y * W_M^E (or conj(W_M^E)) for a general compile-time twiddle: four
 // multiply-adds with immediates.
@@ -471,14 +474,174 @@ __device__ __forceinline__ void fft_stage(T (&x)[PlanInfo<P>::E], const T* __res
   }
 }
 
-template <class P, int K, bool INV, bool HT = false, typename T>
+// The twiddle that forward radix-4 stage SI of pass K puts on register slot
+// s: W_M^(mult (low_r + low_t) 2^sh), mult = 0, 2, 1, 3 for the slot's stage
+// bits 00, 01, 10, 11 (outputs y0 .. y3), low_r its register part, low_t the
+// thread part of the exponent.
+template <class P, int K, int SI> struct StageTw {
+  using I = PlanInfo<P>;
+  static constexpr int dim = P::st[K][SI][0], t = P::st[K][SI][1], lo = P::lo[dim], m = P::m[dim];
+  static constexpr uint32_t lowmask = ((1u << t) - 1u) << lo;
+  static constexpr bool thr_low = (I::thr_mask(K) & lowmask) != 0u;
+  static constexpr int sh = m - t - 2, MM = 1 << m;
+  static constexpr int j0 = I::slot_bit(K, lo + t), j1 = I::slot_bit(K, lo + t + 1);
+  static constexpr int mult(int s) {
+    const int b = ((s >> j0) & 1) | (((s >> j1) & 1) << 1);
+    return b == 0 ? 0 : b == 1 ? 2 : b == 2 ? 1 : 3;
+  }
+  static constexpr int low_r(int s) {
+    return int((uint32_t(I::pos_reg(K, s & ~((1 << j0) | (1 << j1)))) & lowmask) >> lo);
+  }
+  // the stage's butterfly group of slot s (inverse of PlanInfo::insert0)
+  static constexpr int group(int s) {
+    int q = 0, d = 0;
+    for (int j = 0; j < P::e; ++j) {
+      if (j == j0 || j == j1) continue;
+      q |= ((s >> j) & 1) << d;
+      ++d;
+    }
+    return q;
+  }
+  static constexpr int ec(int s) { return mult(s) * (low_r(s) << sh); }  // exponent when !thr_low
+  static constexpr bool none(int s) { return mult(s) == 0 || (!thr_low && ((ec(s) % MM) + MM) % MM == 0); }
+  static constexpr bool general(int s) { return !none(s) && (thr_low || tw_is_general(MM, ec(s))); }
+};
+
+// Forward pass of two radix-4 stages with the first stage's output twiddles
+// deferred to the second stage's inputs (FP32): in each second-stage
+// butterfly the sums x0 + x2, x1 + x3 of twiddled inputs are one product and
+// one multiply-accumulate, the differences 2 t - sum -- 20 FMA-pipe
+// operations instead of 24 per butterfly whose inputs carry general
+// twiddles. The same transform as fft_pass up to rounding, so the inverse is
+// unchanged.
+template <class P, int K, bool HT, typename T>
+__device__ __forceinline__ void fft_pass_fwd_deferred(T (&x)[PlanInfo<P>::E], const T* __restrict__ tw0,
+                                                      const T* __restrict__ tw1, int pos_thr, const T* twr) {
+  using I = PlanInfo<P>;
+  using S1 = StageTw<P, K, 0>;
+  // first stage: butterflies only
+  static_for<I::E / 4>([&](auto Q) {
+    constexpr int s0 = I::insert0(decltype(Q)::value, S1::j0, S1::j1);
+    constexpr int s1 = s0 | (1 << S1::j0), s2 = s0 | (1 << S1::j1), s3 = s0 | (1 << S1::j0) | (1 << S1::j1);
+    const T A = cadd(x[s0], x[s2]), B = cadd(x[s1], x[s3]);
+    const T C = csub(x[s0], x[s2]), D = csub(x[s1], x[s3]);
+    x[s0] = cadd(A, B);
+    x[s1] = csub(A, B);
+    x[s2] = cmake<T>(C.x + D.y, C.y - D.x);  // C - iD
+    x[s3] = cmake<T>(C.x - D.y, C.y + D.x);  // C + iD
+  });
+  const T* __restrict__ tw = S1::dim ? tw1 : tw0;
+  const int low_t = S1::thr_low ? int((uint32_t(pos_thr) & S1::lowmask) >> S1::lo) : 0;
+  // the deferred twiddle of slot s (thread-dependent: table or register set)
+  auto wrt = [&](auto SS) -> T {
+    constexpr int s = decltype(SS)::value;
+    if constexpr (HT) {
+      constexpr int slot = TwSlots<P>::base(K, 0) + 3 * TwSlots<P>::distinct(K, 0, S1::group(s));
+      constexpr int m = S1::mult(s);
+      return twr[slot + (m == 1 ? 0 : m == 2 ? 1 : 2)];
+    } else {
+      return tw[S1::mult(s) * ((S1::low_r(s) + low_t) << S1::sh)];
+    }
+  };
+  // z * w(s)
+  auto dmul = [&](auto SS, T z) -> T {
+    constexpr int s = decltype(SS)::value;
+    if constexpr (S1::none(s)) return z;
+    else if constexpr (S1::thr_low) return cmul(z, wrt(SS));
+    else return cmul_tw<T, S1::MM, S1::ec(s), false>(z);
+  };
+  // acc + z * w(s) for a general twiddle
+  auto dmla = [&](auto SS, T acc, T z) -> T {
+    constexpr int s = decltype(SS)::value;
+    if constexpr (S1::thr_low) {
+      const T w = wrt(SS);
+      return cmlac(acc, z, cmake<T>(w.x, -w.y));
+    } else {
+      return cmla_tw<T, S1::MM, S1::ec(s), false>(acc, z);
+    }
+  };
+  // second stage: twiddled inputs, then its own output twiddles
+  constexpr int SI = 1;
+  using S2 = StageTw<P, K, SI>;
+  const int low_t2 = S2::thr_low ? int((uint32_t(pos_thr) & S2::lowmask) >> S2::lo) : 0;
+  const T* __restrict__ tw2 = S2::dim ? tw1 : tw0;
+  static_for<I::E / 4>([&](auto Q) {
+    constexpr int q = decltype(Q)::value;
+    constexpr int s0 = I::insert0(q, S2::j0, S2::j1);
+    constexpr int s1 = s0 | (1 << S2::j0), s2 = s0 | (1 << S2::j1), s3 = s0 | (1 << S2::j0) | (1 << S2::j1);
+    using C0 = std::integral_constant<int, s0>;
+    using C1 = std::integral_constant<int, s1>;
+    using C2 = std::integral_constant<int, s2>;
+    using C3 = std::integral_constant<int, s3>;
+    T A, B, C, D;
+    const T t0 = dmul(C0{}, x[s0]);
+    if constexpr (S1::general(s2)) {
+      A = dmla(C2{}, t0, x[s2]);
+      C = ctwice_minus(t0, A);
+    } else {
+      const T u = dmul(C2{}, x[s2]);
+      A = cadd(t0, u);
+      C = csub(t0, u);
+    }
+    const T t1 = dmul(C1{}, x[s1]);
+    if constexpr (S1::general(s3)) {
+      B = dmla(C3{}, t1, x[s3]);
+      D = ctwice_minus(t1, B);
+    } else {
+      const T u = dmul(C3{}, x[s3]);
+      B = cadd(t1, u);
+      D = csub(t1, u);
+    }
+    T y0 = cadd(A, B), y1 = csub(A, B);
+    T y2 = cmake<T>(C.x + D.y, C.y - D.x);  // C - iD
+    T y3 = cmake<T>(C.x - D.y, C.y + D.x);  // C + iD
+    constexpr int low_r = int((uint32_t(I::pos_reg(K, s0)) & S2::lowmask) >> S2::lo);
+    constexpr int ec = low_r << S2::sh;
+    if constexpr (S2::thr_low) {
+      T w1, w2, w3;
+      if constexpr (HT) {
+        constexpr int slot = TwSlots<P>::base(K, SI) + 3 * TwSlots<P>::distinct(K, SI, q);
+        w1 = twr[slot];
+        w2 = twr[slot + 1];
+        w3 = twr[slot + 2];
+      } else {
+        const int e1 = (low_r + low_t2) << S2::sh;
+        w1 = tw2[e1];
+        w2 = tw2[2 * e1];
+        w3 = tw2[3 * e1];
+      }
+      y1 = cmul(y1, w2);
+      y2 = cmul(y2, w1);
+      y3 = cmul(y3, w3);
+    } else if constexpr (low_r != 0) {
+      y1 = cmul_tw<T, S2::MM, 2 * ec, false>(y1);
+      y2 = cmul_tw<T, S2::MM, ec, false>(y2);
+      y3 = cmul_tw<T, S2::MM, 3 * ec, false>(y3);
+    }
+    x[s0] = y0; x[s1] = y1; x[s2] = y2; x[s3] = y3;
+  });
+}
+
+// DEF: the single-system kernel (no register cap) takes the deferred
+// first-stage twiddles (fft_pass_fwd_deferred) on the plans below 4096 sites;
+// measured on GB300: 1x2048 1.99e11 -> 2.05e11, 1x1024 2.08e11 -> 2.11e11,
+// 1x256 2.91e11 -> 2.95e11, 16x16 3.33e11 -> 3.36e11 site-updates/s, while
+// 64x64 lost 2 % (251 registers against 240); the batch kernel, at its
+// 128-register cap, keeps the plain passes.
+template <class P, int K, bool INV, bool HT = false, bool DEF = false, typename T>
 __device__ __forceinline__ void fft_pass(T (&x)[PlanInfo<P>::E], const T* tw0, const T* tw1, int pos_thr,
                                          const T* twr = nullptr) {
   constexpr int ns = P::nst[K];
-  static_for<ns>([&](auto S) {
-    constexpr int si = INV ? (ns - 1 - decltype(S)::value) : decltype(S)::value;
-    fft_stage<P, K, si, INV, HT>(x, tw0, tw1, pos_thr, twr);
-  });
+  constexpr bool deferred = DEF && !INV && sizeof(decltype(T::x)) == 4 && P::nbits < 12 && ns == 2 &&
+                            P::st[K][0][2] == 2 && P::st[K][1][2] == 2 && P::st[K][0][1] > 0;
+  if constexpr (deferred) {
+    fft_pass_fwd_deferred<P, K, HT>(x, tw0, tw1, pos_thr, twr);
+  } else {
+    static_for<ns>([&](auto S) {
+      constexpr int si = INV ? (ns - 1 - decltype(S)::value) : decltype(S)::value;
+      fft_stage<P, K, si, INV, HT>(x, tw0, tw1, pos_thr, twr);
+    });
+  }
 }
 
 // The twiddle register set of TwSlots for this thread (table loads, once).
@@ -680,7 +843,7 @@ struct SquareGroup {
           fft_exchange<P, k - 1, k, Cfg::SYNC_WARP>(x, s_x + buf * Cfg::XSZ, xbase[k - 1], xbase[k]);
           buf ^= 1;
         }
-        fft_pass<P, k, false, HT>(x, tw0, tw1, pos_thr[k], twr);
+        fft_pass<P, k, false, HT, REG_SMALL>(x, tw0, tw1, pos_thr[k], twr);
       });
       // k-space multiply by -i 2J (cos kx + cos ky) / N
       static_for<E>([&](auto S) {
