@@ -156,11 +156,11 @@ def measure_warm_start():
     return wsm.evaluate(32, n_train=1024, traj_train=256, t_train=20.0, n_test=64, traj_test=512, t_test=20.0)
 
 
-def make_system(twmc, hop=None, precision=None):
+def make_system(twmc, hop=None, precision=None, integrator=0):
     return twmc.System(nx=NX, ny=NY, J=1.0, gamma=1.0, dt=DT, frame_steps=FRAME_STEPS,
                        omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=0.2, F=2.0, beta_init=0.0,
                        beta_init_sigma=0.5, precision=twmc.PREC_F32 if precision is None else precision,
-                       hop=twmc.HOP_FFT if hop is None else hop, n_moment_blocks=32)
+                       hop=twmc.HOP_FFT if hop is None else hop, n_moment_blocks=32, integrator=integrator)
 
 
 def measure_batch(twmc, torch, sm_mhz=None, t_end=60.0):
@@ -241,10 +241,11 @@ def measure_other_paths(twmc, torch, sm_mhz=None):
     return out
 
 
-def measure_f64(twmc, torch, steps=2):
+def measure_f64(twmc, torch, steps=2, precision=None, integrator=0):
     """The same workload in the engine's FP64 mode (FP64 state, FFT and noise:
-    the plain FP64 GPU split-step), device-timed like the headline."""
-    sysd = make_system(twmc, precision=twmc.PREC_F64)
+    the plain FP64 GPU step; integrator 1 = the exponential split step),
+    device-timed like the headline."""
+    sysd = make_system(twmc, precision=twmc.PREC_F64 if precision is None else precision, integrator=integrator)
     sysd.batch_init(sysd.make_tasks(NTRAJ, t_start=0.0, t_end=T_END, seed0=3, id0=1))
     sysd.advance(FRAME_STEPS)
     sysd.sync()
@@ -568,6 +569,14 @@ def main():
     if world == 1 and args.ntraj == NTRAJ and not args.no_f64:
         f64 = measure_f64(twmc, torch)
         f64["fp32_speedup"] = value / f64["value"]
+        # the exponential split step (TWMC_INTEGRATOR_SPLIT) in FP64, the
+        # target's plain FP64 GPU split-step, and the same step in FP32
+        sp = measure_f64(twmc, torch, integrator=twmc.INTEGRATOR_SPLIT)
+        sp["fp32_speedup"] = value / sp["value"]
+        sp32 = measure_f64(twmc, torch, precision=twmc.PREC_F32, integrator=twmc.INTEGRATOR_SPLIT)
+        sp["fp32_split_step"] = {"value": sp32["value"], "kernel": sp32["kernel"],
+                                 "vs_fp64_split": sp32["value"] / sp["value"]}
+        f64["split_step"] = sp
     obs_err = None
     if world == 1 and args.ntraj == NTRAJ and not args.no_obs_err:
         obs_err = measure_observable_error(twmc)

@@ -35,7 +35,7 @@
 extern "C" {
 #endif
 
-#define TWMC_ABI_VERSION 2
+#define TWMC_ABI_VERSION 3
 
 #if defined(__GNUC__)
 #define TWMC_API __attribute__((visibility("default")))
@@ -70,6 +70,14 @@ enum twmc_noise_mode {
 enum twmc_hop_mode {
   TWMC_HOP_FFT = 0,     /* square lattice: on-chip FFT, k-space multiply, inverse FFT (the reference's algorithm) */
   TWMC_HOP_STENCIL = 1  /* square lattice: the same operator applied in real space (nearest neighbours) */
+};
+
+enum twmc_integrator {
+  TWMC_INTEGRATOR_EULER = 0, /* the reference's step (TWMCBaseSolver.cpp:232-266): the hopping h = IFFT(-i 2J c_k
+                                FFT(beta)) / N enters the Euler-Maruyama increment with the local terms */
+  TWMC_INTEGRATOR_SPLIT = 1  /* exponential split step: beta' = IFFT(exp(-i 2J c_k dt) FFT(beta)) / N (the
+                                hopping integrated exactly over dt), then the Euler-Maruyama local step on beta'
+                                (square lattice, FFT path only) */
 };
 
 enum twmc_ic_kind {
@@ -120,6 +128,8 @@ typedef struct twmc_system_desc {
    *   dF/dt = Re(F(t) - F(t - dt)) / dt (0 on a run's first step),
    * b the field after the step. Runs on the real-space kernel. */
   int32_t thermo;
+  int32_t integrator;  /* twmc_integrator (TWMC_INTEGRATOR_SPLIT needs the FFT path: square lattice, hop_mode
+                          FFT, power-of-two sides of a compiled plan, no F(t), no work / area) */
 } twmc_system_desc;
 
 typedef struct twmc_task_desc {

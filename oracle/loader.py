@@ -22,6 +22,7 @@ def _setup(lib):
     lib.orc_base_run.argtypes = [C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_int64, C.c_int64, C.c_int, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                  C.c_int, C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p]
+    lib.orc_split_run.argtypes = lib.orc_base_run.argtypes
     lib.orc_lieb_run.argtypes = [C.c_int64, C.c_int, C.c_double, C.c_double, C.c_double, C.c_double, C.c_double,
                                  C.c_double, C.c_double, C.c_int64, C.c_int64, C.c_int, C.c_void_p, C.c_void_p,
                                  C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_void_p,
@@ -85,17 +86,18 @@ NOISE = {"buffer": 0, "philox64": 1, "philox32": 2, "mt19937": 3}
 
 
 def base_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, store_initial, omega, U, F, beta0,
-             xi=None, seed=0, tid=0, noise="buffer", fast=False):
+             xi=None, seed=0, tid=0, noise="buffer", fast=False, integrator="euler"):
     n = nx * ny
     om, u, f = (_c(np.broadcast_to(v, (n,))) for v in (omega, U, F))
     beta = _c(beta0).copy()
     frames = np.zeros((max(n_frames, 1), n), dtype=np.complex128)
     meta = np.zeros(3)
     xi_c = _c(xi) if xi is not None else None
-    load(fast).orc_base_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, int(store_initial),
-                            om.ctypes.data, u.ctypes.data, f.ctypes.data, beta.ctypes.data, NOISE[noise],
-                            None if xi_c is None else xi_c.ctypes.data, seed, tid, frames.ctypes.data,
-                            meta.ctypes.data)
+    lib = load(fast)
+    run = {"euler": lib.orc_base_run, "split": lib.orc_split_run}[integrator]
+    run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, int(store_initial),
+        om.ctypes.data, u.ctypes.data, f.ctypes.data, beta.ctypes.data, NOISE[noise],
+        None if xi_c is None else xi_c.ctypes.data, seed, tid, frames.ctypes.data, meta.ctypes.data)
     return {"frames": frames[: int(meta[0])], "final": beta, "frames_written": int(meta[0]), "t_final": meta[1],
             "steps": int(meta[2])}
 

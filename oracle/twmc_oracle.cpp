@@ -377,7 +377,8 @@ static int square_run(int64_t nx, int64_t ny, double J, double gamma, double dt,
                       int64_t frame_steps, int64_t n_frames, int store_initial, const double* omega_ri,
                       const double* U_ri, const double* F_ri, int64_t ft_nrec, const double* ft_times,
                       const double* ft_vals_ri, double* beta_ri, int noise_mode, const double* xi_ri, uint32_t seed,
-                      uint32_t tid, double* frames_ri, double* work, double* area, double* out_meta) {
+                      uint32_t tid, double* frames_ri, double* work, double* area, double* out_meta,
+                      bool split = false) {
   const int64_t n = nx * ny;
   cd* beta = reinterpret_cast<cd*>(beta_ri);
   const cd* omega = reinterpret_cast<const cd*>(omega_ri);
@@ -393,6 +394,9 @@ static int square_run(int64_t nx, int64_t ny, double J, double gamma, double dt,
       kstep[size_t(i * ny + j)] = -ij * 2.0 * J *
                                   (f1x * std::cos(2.0 * M_PI / double(nx) * double(i)) +
                                    f1y * std::cos(2.0 * M_PI / double(ny) * double(j)));
+  // split step: the hopping integrated exactly over dt, exp(kstep dt) = exp(-i 2J c_k dt)
+  std::vector<cd> kprop(static_cast<size_t>(split ? n : 0));
+  for (int64_t i = 0; split && i < n; ++i) kprop[size_t(i)] = std::exp(kstep[size_t(i)] * dt);
   const double norm = double(n);
   const double dt4 = std::sqrt(gamma * dt / 4.0);
   std::vector<cd> fin(static_cast<size_t>(n)), a(static_cast<size_t>(n)), xi(static_cast<size_t>(n));
@@ -422,9 +426,16 @@ static int square_run(int64_t nx, int64_t ny, double J, double gamma, double dt,
     }
     fin.assign(beta, beta + n);
     fft2d(fin.data(), nx, ny, -1);
-    for (int64_t i = 0; i < n; ++i) fin[size_t(i)] = kstep[size_t(i)] * fin[size_t(i)];
-    fft2d(fin.data(), nx, ny, +1);
-    for (int64_t i = 0; i < n; ++i) fin[size_t(i)] = fin[size_t(i)] / norm;
+    if (split) {  // beta' = IFFT(exp(-i 2J c_k dt) FFT(beta)) / N, then the local step on beta'
+      for (int64_t i = 0; i < n; ++i) fin[size_t(i)] = kprop[size_t(i)] * fin[size_t(i)];
+      fft2d(fin.data(), nx, ny, +1);
+      for (int64_t i = 0; i < n; ++i) beta[i] = fin[size_t(i)] / norm;
+      std::fill(fin.begin(), fin.end(), cd(0.0, 0.0));
+    } else {
+      for (int64_t i = 0; i < n; ++i) fin[size_t(i)] = kstep[size_t(i)] * fin[size_t(i)];
+      fft2d(fin.data(), nx, ny, +1);
+      for (int64_t i = 0; i < n; ++i) fin[size_t(i)] = fin[size_t(i)] / norm;
+    }
     for (int64_t i = 0; i < n; ++i) {
       const double ab2 = beta[i].real() * beta[i].real() + beta[i].imag() * beta[i].imag();
       a[size_t(i)] = ((rsl[size_t(i)] + ij * U[i] * (ab2 - 1.0)) * beta[i] + fin[size_t(i)] + ij * F[size_t(i)]) * dt;
@@ -490,6 +501,20 @@ int orc_base_run(int64_t nx, int64_t ny, double J, double gamma, double dt, doub
                  uint32_t seed, uint32_t tid, double* frames_ri, double* out_meta) {
   return square_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, store_initial, omega_ri, U_ri, F_ri,
                     0, nullptr, nullptr, beta_ri, noise_mode, xi_ri, seed, tid, frames_ri, nullptr, nullptr, out_meta);
+}
+
+// The same trajectory with the exponential split step of the engine's
+// TWMC_INTEGRATOR_SPLIT (an optional mode; the reference integrates the
+// hopping by the Euler step above): beta' = IFFT(exp(-i 2J c_k dt) FFT(beta)) / N,
+// then a = ((rsl + iU (|beta'|^2 - 1)) beta' + iF) dt and
+// beta = beta' + a + sqrt(gamma dt / 4) xi. Arguments as orc_base_run.
+int orc_split_run(int64_t nx, int64_t ny, double J, double gamma, double dt, double t_start, double t_end,
+                  int64_t frame_steps, int64_t n_frames, int store_initial, const double* omega_ri,
+                  const double* U_ri, const double* F_ri, double* beta_ri, int noise_mode, const double* xi_ri,
+                  uint32_t seed, uint32_t tid, double* frames_ri, double* out_meta) {
+  return square_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, store_initial, omega_ri, U_ri, F_ri,
+                    0, nullptr, nullptr, beta_ri, noise_mode, xi_ri, seed, tid, frames_ri, nullptr, nullptr, out_meta,
+                    true);
 }
 
 // The square-lattice loop with an F(t) table (evaluated at the pre-step t, as

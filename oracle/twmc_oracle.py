@@ -84,8 +84,10 @@ def kstep_table(nx: int, ny: int, J: float) -> np.ndarray:
 
 
 def base_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, store_initial, omega, U, F, beta0,
-             xi=None, seed=0, tid=0, noise="buffer"):
-    """One trajectory of the 1-D/2-D solver; returns (frames, beta_final, t_final, steps)."""
+             xi=None, seed=0, tid=0, noise="buffer", integrator="euler"):
+    """One trajectory of the 1-D/2-D solver; returns (frames, beta_final, t_final, steps).
+    integrator "split": the engine's optional exponential split step, beta' =
+    ifft2(exp(k_step dt) fft2(beta)), then the local step on beta'."""
     n = nx * ny
     beta = np.array(beta0, dtype=np.complex128).reshape(nx, ny)
     rsl = (-1j * np.broadcast_to(np.asarray(omega), (n,)).reshape(nx, ny) - gamma / 2.0)
@@ -101,7 +103,11 @@ def base_run(nx, ny, J, gamma, dt, t_start, t_end, frame_steps, n_frames, store_
         i_frame = 1
     t = t_start
     while t <= t_end:
-        hop = np.fft.ifft2(ks * np.fft.fft2(beta))  # ifft2 includes the 1/N
+        if integrator == "split":
+            beta = np.fft.ifft2(np.exp(ks * dt) * np.fft.fft2(beta))
+            hop = 0.0
+        else:
+            hop = np.fft.ifft2(ks * np.fft.fft2(beta))  # ifft2 includes the 1/N
         a = ((rsl + 1j * U * (np.abs(beta) ** 2 - 1.0)) * beta + hop + 1j * F) * dt
         if noise == "buffer":
             z = np.asarray(xi[i_step]).reshape(nx, ny)

@@ -93,6 +93,7 @@ struct twmc_handle {
   // F(t)
   bool timedep = false;
   bool thermo = false;     // work / area accumulators (TWMCThermoSolver)
+  int integrator = TWMC_INTEGRATOR_EULER;
   DevBuf d_work, d_area;
   DevBuf d_wide;           // FP32 -> FP64 download staging (bounded chunk)
   // final-field pipeline of twmc_run: the last steps run in kFinalChunks
@@ -112,7 +113,7 @@ struct twmc_handle {
   int bx = 0, by = 0;
   std::string kname;
   // device tables
-  DevBuf d_tw, d_ktab, d_nbr_idx, d_nbr_w, d_ft_vals, d_ft_slopes, d_ft_id, d_ft_dt, d_ft_dt_f;
+  DevBuf d_tw, d_ktab, d_kfac, d_nbr_idx, d_nbr_w, d_ft_vals, d_ft_slopes, d_ft_id, d_ft_dt, d_ft_dt_f;
   DevBuf d_shared_par[3];  // shared per-site rsl / iU / iF when not per-trajectory
   // batch
   int64_t ntraj = 0;
@@ -305,6 +306,26 @@ int build_tables(twmc_handle* h) {
     for (int64_t k = 0; k < M0; ++k) kt.push_back(scale * fy * std::cos(2.0 * M_PI / double(h->ny) * double(k)));
     for (int64_t k = 0; k < M1; ++k) kt.push_back(scale * fx * std::cos(2.0 * M_PI / double(h->nx) * double(k)));
     if (!upload_r(&h->d_ktab, kt, prec)) return fail(h, TWMC_ERR_NOMEM, "k table upload");
+    if (h->integrator == TWMC_INTEGRATOR_SPLIT) {
+      // (exp(-i theta) - 1) / N, theta = 2J (fx cos(2 pi kx / nx) + fy cos(2 pi ky / ny)) dt, at every
+      // position p of the forward plan's output (frequencies bit-reversed per dimension);
+      // cos(theta) - 1 as -2 sin^2(theta / 2), free of cancellation
+      auto bitrev = [](int64_t v, int nb) {
+        int64_t r = 0;
+        for (int i = 0; i < nb; ++i) r |= ((v >> i) & 1) << (nb - 1 - i);
+        return r;
+      };
+      std::vector<cd> kf(size_t(h->nsites));
+      for (int64_t p = 0; p < h->nsites; ++p) {
+        const int64_t ky = bitrev(p & (M0 - 1), h->by), kx = h->bx ? bitrev(p >> h->by, h->bx) : 0;
+        const double th = 2.0 * h->J * h->dt *
+                          (fx * std::cos(2.0 * M_PI / double(h->nx) * double(kx)) +
+                           fy * std::cos(2.0 * M_PI / double(h->ny) * double(ky)));
+        const double sh = std::sin(0.5 * th);
+        kf[size_t(p)] = cd(-2.0 * sh * sh, -std::sin(th)) / double(h->nsites);
+      }
+      if (!upload_c(&h->d_kfac, kf, prec)) return fail(h, TWMC_ERR_NOMEM, "split-step table upload");
+    }
   } else if (h->lattice == TWMC_LATTICE_LIEB) {
     // Coupling triplets of TWMCLiebSolver::Setup (TWMCLiebSolver.cpp:54-85).
     const int64_t nc = h->nsites / 3;
@@ -428,6 +449,7 @@ int advance(twmc_handle* h, int64_t n, bool want_nk, int64_t t0 = 0, int64_t t1 
   a.status = h->d_status.as<int>() + t0;
   a.tw = h->d_tw.p;
   a.ktab = h->d_ktab.p;
+  a.kfac = h->integrator == TWMC_INTEGRATOR_SPLIT ? h->d_kfac.p : nullptr;
   a.nsites = h->nsites;
   a.nx = h->lattice == TWMC_LATTICE_SQUARE ? h->nx : 1;
   a.ny = h->lattice == TWMC_LATTICE_SQUARE ? h->ny : h->nsites;
@@ -708,6 +730,10 @@ int validate_desc(const twmc_system_desc* d, std::string* why) {
     *why = "noise on beta_init / beta_init_sigma is not supported";
     return TWMC_ERR_INVALID;
   }
+  if (d->integrator != TWMC_INTEGRATOR_EULER && d->integrator != TWMC_INTEGRATOR_SPLIT) {
+    *why = "unknown integrator";
+    return TWMC_ERR_INVALID;
+  }
   if (d->thermo != 0 && d->lattice != TWMC_LATTICE_SQUARE) {
     *why = "work / area accumulation is defined for the square lattice only";
     return TWMC_ERR_INVALID;
@@ -760,11 +786,18 @@ int twmc_create(const twmc_system_desc* d, twmc_handle** out) {
       build_time_table(h, d->ft_times, d->ft_values, d->ft_nrec);
     }
     h->thermo = d->thermo != 0;
+    h->integrator = d->integrator;
     setup_params(h);
     if (h->lattice == TWMC_LATTICE_SQUARE && h->hop_mode == TWMC_HOP_FFT && !h->timedep && !h->thermo) {
       const int bx = ilog2_exact(h->nx), by = ilog2_exact(h->ny);
       PlanView pv;
       if (bx >= 0 && by >= 0 && square_plan(bx, by, &pv)) { h->use_fft = true; h->bx = bx; h->by = by; }
+    }
+    if (h->integrator == TWMC_INTEGRATOR_SPLIT && !h->use_fft) {
+      h->err = "the split-step integrator needs the FFT path (square lattice, hop_mode FFT, power-of-two sides "
+               "of a compiled plan, no F(t), no work / area)";
+      *out = h;
+      return TWMC_ERR_INVALID;
     }
     h->kname = h->use_fft ? "square_fft_kernel" : (h->lattice == TWMC_LATTICE_LIEB ? "ell_kernel<table>" : "ell_kernel<stencil>");
     if (!h->use_fft && h->lattice == TWMC_LATTICE_SQUARE && h->prec == TWMC_PREC_F32 && h->nsites > 8192 &&

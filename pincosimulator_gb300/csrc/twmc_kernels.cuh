@@ -53,6 +53,9 @@ struct StepArgs {
   // square FFT kernel tables
   const void* tw;         // [M0 + M1] complex R: W_M^j per dimension
   const void* ktab;       // [M0 + M1] R: 2J cos(2 pi k / n) / N per dimension (columns, then rows)
+  const void* kfac;       // exponential split step: [N] complex R, (exp(-i 2J c_k dt) - 1) / N at each
+                          // position of the forward plan's output; NULL = the Euler step
+  int kfac_smem;          // split step: 1 = table copied to shared memory, 0 = read from global (L2)
   // ell kernel
   int tpt;                // threads per trajectory
   int64_t nsites;         // N
@@ -717,6 +720,10 @@ struct SquareCfg {
     return sizeof(T) * (size_t(I::TW0 + I::TW1) + 2 * size_t(XSZ) + (BETA_SMEM ? size_t(TPC) * N : 0)) +
            sizeof(R) * size_t(I::M0 + I::M1);
   }
+  // the split-step factor table behind the rest (16-byte aligned, padded
+  // like the exchange buffers), present only when a launch passes kfac
+  static constexpr size_t kfac_offset() { return (smem_bytes() + 15) & ~size_t(15); }
+  static constexpr size_t smem_bytes_split() { return kfac_offset() + sizeof(c2_t<R>) * size_t(N + N / 16); }
 };
 
 // One square-lattice trajectory group (TPC trajectories) for a.nsteps steps:
@@ -740,6 +747,7 @@ struct SquareGroup {
   T* s_x;
   T* s_beta;
   R* s_kt;
+  T* s_kf;
   int tid, slot, t;
   int pos_thr[NP];
   int xbase[NP];
@@ -749,6 +757,7 @@ struct SquareGroup {
     s_x = s_tw + (I::TW0 + I::TW1);
     s_beta = s_x + 2 * Cfg::XSZ;
     s_kt = reinterpret_cast<R*>(s_beta + (BETA_SMEM ? TPC * N : 0));
+    s_kf = reinterpret_cast<T*>(smem_raw + Cfg::kfac_offset());
     tid = threadIdx.x;
     // one trajectory per CTA: the trajectory index (and its Philox key) is
     // uniform across the CTA
@@ -772,6 +781,8 @@ struct SquareGroup {
     for (int i = tid; i < I::TW0; i += CTA) s_tw[i] = reinterpret_cast<const T*>(a.tw)[i];
     for (int i = tid; i < I::TW1; i += CTA) s_tw[I::TW0 + i] = reinterpret_cast<const T*>(a.tw)[I::M0 + i];
     for (int i = tid; i < I::M0 + I::M1; i += CTA) s_kt[i] = reinterpret_cast<const R*>(a.ktab)[i];
+    if (!FAST && a.kfac != nullptr && a.kfac_smem)
+      for (int i = tid; i < N; i += CTA) s_kf[pad16(i)] = reinterpret_cast<const T*>(a.kfac)[i];
   }
 
   __device__ __forceinline__ void run(const StepArgs& a, int64_t g, int& buf) {
@@ -784,6 +795,11 @@ struct SquareGroup {
     const R* s_ky = s_kt + ky_t;
     const R* s_kx = s_kt + I::M0 + kx_t;
     const R kx_const = s_kx[0];  // used when no register bit is a row bit
+    // split step (general instantiation only): the factor table, thread part
+    // of the padded position in the last pass's layout
+    const bool split = !FAST && a.kfac != nullptr;
+    const int kf_thr = pad16(pos_thr[LAST]);
+    const T* __restrict__ g_kf = reinterpret_cast<const T*>(a.kfac);
     const R dt = sizeof(R) == 4 ? R(a.f_dt) : R(a.dt), dt4 = sizeof(R) == 4 ? R(a.f_dt4) : R(a.dt4);
     const T rsl_s = sizeof(R) == 4 ? cmake<T>(R(a.f_par[0]), R(a.f_par[1])) : cmake<T>(R(a.rsl_s[0]), R(a.rsl_s[1]));
     const T iU_s = sizeof(R) == 4 ? cmake<T>(R(a.f_par[2]), R(a.f_par[3])) : cmake<T>(R(a.iU_s[0]), R(a.iU_s[1]));
@@ -845,14 +861,30 @@ struct SquareGroup {
         }
         fft_pass<P, k, false, HT, REG_SMALL>(x, tw0, tw1, pos_thr[k], twr);
       });
-      // k-space multiply by -i 2J (cos kx + cos ky) / N
-      static_for<E>([&](auto S) {
-        constexpr int s = decltype(S)::value;
-        constexpr int pr = I::pos_reg(LAST, s);
-        R sk = s_ky[I::ky_of(pr)];
-        if constexpr (I::last_has_row_reg()) sk += s_kx[I::kx_of(pr)]; else sk += kx_const;
-        x[s] = cmake<T>(sk * x[s].y, -sk * x[s].x);
-      });
+      // k-space multiply by -i 2J (cos kx + cos ky) / N (Euler), or by
+      // (exp(-i 2J (cos kx + cos ky) dt) - 1) / N (split step: the inverse
+      // transform is then beta' - beta)
+      if (split) {
+        if (a.kfac_smem) {
+          static_for<E>([&](auto S) {
+            constexpr int s = decltype(S)::value;
+            x[s] = cmul(x[s], s_kf[kf_thr + pad16(I::pos_reg(LAST, s))]);
+          });
+        } else {
+          static_for<E>([&](auto S) {
+            constexpr int s = decltype(S)::value;
+            x[s] = cmul(x[s], __ldg(g_kf + (pos_thr[LAST] | I::pos_reg(LAST, s))));
+          });
+        }
+      } else {
+        static_for<E>([&](auto S) {
+          constexpr int s = decltype(S)::value;
+          constexpr int pr = I::pos_reg(LAST, s);
+          R sk = s_ky[I::ky_of(pr)];
+          if constexpr (I::last_has_row_reg()) sk += s_kx[I::kx_of(pr)]; else sk += kx_const;
+          x[s] = cmake<T>(sk * x[s].y, -sk * x[s].x);
+        });
+      }
       // inverse FFT (adjoint passes in reverse order)
       static_for<NP>([&](auto KK) {
         constexpr int k = LAST - decltype(KK)::value;
@@ -888,7 +920,17 @@ struct SquareGroup {
         constexpr std::integral_constant<int, s_lo> SL{};
         constexpr std::integral_constant<int, s_hi> SH{};
         T n_lo, n_hi;
-        if constexpr (sizeof(R) == 4) {  // dt is folded into the k-space table
+        if (split) {  // the local step on beta' = beta + (beta' - beta), no hopping term
+          const T zero = cmake<T>(R(0), R(0));
+          const T b_lo = cadd(bget(SL), x[s_lo]), b_hi = cadd(bget(SH), x[s_hi]);
+          if constexpr (sizeof(R) == 4) {
+            n_lo = local_update_fused(b_lo, zero, r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo);
+            n_hi = local_update_fused(b_hi, zero, r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi);
+          } else {
+            n_lo = local_update(b_lo, zero, r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo);
+            n_hi = local_update(b_hi, zero, r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi);
+          }
+        } else if constexpr (sizeof(R) == 4) {  // dt is folded into the k-space table
           n_lo = local_update_fused<HT>(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo);
           n_hi = local_update_fused<HT>(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi);
         } else {

@@ -28,11 +28,14 @@ bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo*
   constexpr int CTA = cta_for<R, P>();
   using Cfg = SquareCfg<P, CTA, R, true>;  // as square_fft_kernel instantiates it
   (void)nparams;
-  const StepArgs a2 = a;
-  const size_t smem = Cfg::smem_bytes();
+  StepArgs a2 = a;
   int dev0 = 0, maxsm = 0;
   cudaGetDevice(&dev0);
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev0);
+  // the split-step table goes to shared memory where it fits (FP64 4096-site
+  // plans read it from global memory)
+  a2.kfac_smem = (!FAST && a.kfac != nullptr && Cfg::smem_bytes_split() <= size_t(maxsm)) ? 1 : 0;
+  const size_t smem = a2.kfac_smem ? Cfg::smem_bytes_split() : Cfg::smem_bytes();
   if (smem > size_t(maxsm)) {
     if (err) *err = "square kernel needs " + std::to_string(smem) + " B of shared memory (device max " +
                     std::to_string(maxsm) + ")";
@@ -76,8 +79,8 @@ bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo*
 template <typename R>
 bool square_dispatch(int bx, int by, const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo* info,
                      std::string* err) {
-  // FP32 runs with Philox noise and scalar U, F take the fast instantiation
-  const bool fast = sizeof(R) == 4 && a.noise_mode == 0 && a.iU == nullptr && a.iF == nullptr;
+  // FP32 Euler runs with Philox noise and scalar U, F take the fast instantiation
+  const bool fast = sizeof(R) == 4 && a.noise_mode == 0 && a.iU == nullptr && a.iF == nullptr && a.kfac == nullptr;
 #define TWMC_SHAPE(BX, BY)                                                                          \
   if (bx == BX && by == BY)                                                                         \
     return fast ? square_launch_t<R, Plan_##BX##_##BY, sizeof(R) == 4>(a, nparams, s, info, err)   \

@@ -67,6 +67,7 @@ TWMCSystemData::TWMCSystemData(const Settings& s) {
   if (dt_obs < dt) { dt_obs = dt; frame_steps = 1; }
   precision = s.getString("precision", "f32");
   hop = s.getString("hop", "fft");
+  integrator = s.getString("integrator", "euler");
 }
 
 size_t TWMCSystemData::ComputeNFrames(double ts, double te) const {
@@ -214,6 +215,7 @@ void TWMCCudaSolver::SetupFor(const TWMCSystemData* d) {
   desc.precision = d->precision == "f64" ? TWMC_PREC_F64 : TWMC_PREC_F32;
   desc.noise_mode = TWMC_NOISE_PHILOX;
   desc.hop_mode = d->hop == "stencil" ? TWMC_HOP_STENCIL : TWMC_HOP_FFT;
+  desc.integrator = d->integrator == "split" ? TWMC_INTEGRATOR_SPLIT : TWMC_INTEGRATOR_EULER;
   // the reference's manager runs a periodic lattice with F(t) on its Thermo
   // solver, which adds the work and area datasets (TWMCManager.cpp:47-58)
   thermo_ = !lieb && d->F.HasTimeDependence();

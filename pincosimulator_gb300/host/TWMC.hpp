@@ -48,6 +48,7 @@ class TWMCSystemData {
   // engine options (keys absent from the reference's inputs)
   std::string precision = "f32";  // "f32" | "f64"
   std::string hop = "fft";        // "fft" | "stencil"
+  std::string integrator = "euler";  // "euler" (the reference's step) | "split" (exact hopping over dt)
   size_t n_sites() const { return nx * ny * cellSz; }
 };
 

@@ -22,6 +22,7 @@ LATTICE_SQUARE, LATTICE_LIEB = 0, 1
 PREC_F32, PREC_F64 = 0, 1
 NOISE_PHILOX, NOISE_BUFFER = 0, 1
 HOP_FFT, HOP_STENCIL = 0, 1
+INTEGRATOR_EULER, INTEGRATOR_SPLIT = 0, 1
 IC_SETTINGS, IC_FIXED, IC_GIVEN = 0, 1, 2
 DISORDER_NONE, DISORDER_GAUSSIAN, DISORDER_UNIFORM = 0, 1, 2
 
@@ -52,7 +53,7 @@ class SystemDesc(C.Structure):
         ("omega", Matrix), ("U", Matrix), ("F", Matrix), ("beta_init", Matrix), ("beta_init_sigma", Matrix),
         ("ft_nrec", C.c_int64), ("ft_times", C.c_void_p), ("ft_values", C.c_void_p),
         ("precision", C.c_int32), ("noise_mode", C.c_int32), ("hop_mode", C.c_int32), ("n_moment_blocks", C.c_int32),
-        ("thermo", C.c_int32),
+        ("thermo", C.c_int32), ("integrator", C.c_int32),
     ]
 
 
@@ -201,7 +202,7 @@ class System:
     def __init__(self, *, lattice=LATTICE_SQUARE, nx=1, ny=1, pbc=True, J=0.0, J_AB=0.0, J_BC=0.0, gamma=1.0,
                  detuning=0.0, dt=0.01, frame_steps=1, omega=0.0, U=0.0, F=0.0, beta_init=0.0, beta_init_sigma=0.0,
                  F_t: Optional[tuple] = None, precision=PREC_F32, noise=NOISE_PHILOX, hop=HOP_FFT, n_moment_blocks=32,
-                 thermo=False):
+                 thermo=False, integrator=INTEGRATOR_EULER):
         self.lib = load()
         self.n_sites = (3 if lattice == LATTICE_LIEB else 1) * nx * ny
         n = self.n_sites
@@ -225,6 +226,7 @@ class System:
             d.ft_nrec, d.ft_times, d.ft_values = len(times), times.ctypes.data, vals.ctypes.data
         d.precision, d.noise_mode, d.hop_mode, d.n_moment_blocks = precision, noise, hop, n_moment_blocks
         d.thermo = int(bool(thermo))
+        d.integrator = integrator
         self.thermo = bool(thermo)
         self.desc = d
         self.n_blocks = n_moment_blocks

@@ -11,7 +11,7 @@ def rel_err(a, b):
 
 
 def square_case(orc, nx, ny, *, ntraj=3, steps=200, dt=0.005, frame_steps=50, J=1.0, gamma=1.0, omega=-0.5,
-                U=0.2, F=1.5, prec=twmc.PREC_F32, hop=twmc.HOP_FFT, seed=0, amp=0.4):
+                U=0.2, F=1.5, prec=twmc.PREC_F32, hop=twmc.HOP_FFT, seed=0, amp=0.4, integrator="euler"):
     """Deterministic-noise run of ntraj trajectories: returns (gpu result, oracle results)."""
     n = nx * ny
     rng = np.random.default_rng(seed + 1000 * nx + ny)
@@ -20,10 +20,11 @@ def square_case(orc, nx, ny, *, ntraj=3, steps=200, dt=0.005, frame_steps=50, J=
     t_end = steps * dt
     n_frames = int(round(t_end / (dt * frame_steps))) + 1
     refs = [orc.base_run(nx, ny, J, gamma, dt, 0.0, t_end, frame_steps, n_frames, True, omega, U, F, beta0[k],
-                         xi=xi[k]) for k in range(ntraj)]
+                         xi=xi[k], integrator=integrator) for k in range(ntraj)]
     S = refs[0]["steps"]
     sysd = twmc.System(nx=nx, ny=ny, J=J, gamma=gamma, dt=dt, frame_steps=frame_steps, omega=omega, U=U, F=F,
-                       precision=prec, noise=twmc.NOISE_BUFFER, hop=hop)
+                       precision=prec, noise=twmc.NOISE_BUFFER, hop=hop,
+                       integrator={"euler": twmc.INTEGRATOR_EULER, "split": twmc.INTEGRATOR_SPLIT}[integrator])
     tasks = sysd.make_tasks(ntraj, t_start=0.0, t_end=t_end, ic=twmc.IC_GIVEN, init_field=beta0)
     sysd.set_noise(xi[:, :S])
     res = sysd.run(tasks, frames=True)

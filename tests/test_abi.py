@@ -20,7 +20,7 @@ def test_header_declares_entry_points():
 def test_library_exports_all_declared(built_lib):
     for s in declared_symbols():
         assert hasattr(built_lib, s), s
-    assert built_lib.twmc_version() == 2
+    assert built_lib.twmc_version() == 3
 
 
 def test_binding_lists_every_export():
