@@ -210,7 +210,8 @@ TWMC_API int twmc_batch_download(twmc_handle* h, double* field, double* moments)
 TWMC_API int64_t twmc_launch_count(const twmc_handle* h);
 /* Name of the step kernel variant the handle selected: "square_fft_kernel"
  * (register FFT; "square_fft_kernel<fast>" for its compiled-in common run:
- * FP32, Philox noise, scalar U and F), "ell_kernel<stencil>" / "ell_kernel<table>" (real space,
+ * FP32, Philox noise, scalar U and F; "square_fft_kernel<fast,split>" the same
+ * with the split-step integrator), "ell_kernel<stencil>" / "ell_kernel<table>" (real space,
  * square stencil / Lieb neighbour table), "rowrun_kernel" (square stencil,
  * 4096 sites, FP32 Philox runs), "lieb_cell_kernel" (Lieb lattice, even
  * number of cells), "ell_cluster_pow2_kernel" / "ell_cluster_kernel" (square

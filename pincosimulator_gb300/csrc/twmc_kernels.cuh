@@ -731,7 +731,7 @@ struct SquareCfg {
 // Shared memory: twiddles | 2 padded exchange buffers | state slices (FP32) |
 // separable k-space table. FAST: Philox noise and scalar U, F (per-site
 // omega allowed) compiled in instead of tested per site.
-template <typename R, class P, int CTA, bool FAST = false, bool REG_SMALL = false>
+template <typename R, class P, int CTA, bool FAST = false, bool REG_SMALL = false, bool SPLIT = false>
 struct SquareGroup {
   using T = c2_t<R>;
   using I = PlanInfo<P>;
@@ -781,7 +781,7 @@ struct SquareGroup {
     for (int i = tid; i < I::TW0; i += CTA) s_tw[i] = reinterpret_cast<const T*>(a.tw)[i];
     for (int i = tid; i < I::TW1; i += CTA) s_tw[I::TW0 + i] = reinterpret_cast<const T*>(a.tw)[I::M0 + i];
     for (int i = tid; i < I::M0 + I::M1; i += CTA) s_kt[i] = reinterpret_cast<const R*>(a.ktab)[i];
-    if (!FAST && a.kfac != nullptr && a.kfac_smem)
+    if ((SPLIT || !FAST) && a.kfac != nullptr && a.kfac_smem)
       for (int i = tid; i < N; i += CTA) s_kf[pad16(i)] = reinterpret_cast<const T*>(a.kfac)[i];
   }
 
@@ -795,9 +795,10 @@ struct SquareGroup {
     const R* s_ky = s_kt + ky_t;
     const R* s_kx = s_kt + I::M0 + kx_t;
     const R kx_const = s_kx[0];  // used when no register bit is a row bit
-    // split step (general instantiation only): the factor table, thread part
-    // of the padded position in the last pass's layout
-    const bool split = !FAST && a.kfac != nullptr;
+    // split step (compiled in with SPLIT, tested at run time by the general
+    // instantiation): the factor table, thread part of the padded position
+    // in the last pass's layout
+    const bool split = SPLIT ? true : (FAST ? false : a.kfac != nullptr);
     const int kf_thr = pad16(pos_thr[LAST]);
     const T* __restrict__ g_kf = reinterpret_cast<const T*>(a.kfac);
     const R dt = sizeof(R) == 4 ? R(a.f_dt) : R(a.dt), dt4 = sizeof(R) == 4 ? R(a.f_dt4) : R(a.dt4);
@@ -989,10 +990,10 @@ struct SquareGroup {
 // SM, which measured 7 % (64x64) and 17 % (1x4096) faster than two CTAs per
 // SM at a 128-register cap with spills; the smaller plans stay below 128
 // registers either way.
-template <typename R, class P, int CTA, bool FAST = false>
+template <typename R, class P, int CTA, bool FAST = false, bool SPLIT = false>
 __global__ void __launch_bounds__(CTA, 1) square_fft_kernel(const StepArgs a) {
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  using G = SquareGroup<R, P, CTA, FAST, true>;
+  using G = SquareGroup<R, P, CTA, FAST, true, SPLIT>;
   G grp(smem_raw);
   grp.load_tables(a);
   __syncthreads();

@@ -23,7 +23,7 @@ constexpr int cta_for() {
   return tpc * tpt;
 }
 
-template <typename R, class P, bool FAST>
+template <typename R, class P, bool FAST, bool SPLIT = false>
 bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo* info, std::string* err) {
   constexpr int CTA = cta_for<R, P>();
   using Cfg = SquareCfg<P, CTA, R, true>;  // as square_fft_kernel instantiates it
@@ -34,14 +34,14 @@ bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo*
   cudaDeviceGetAttribute(&maxsm, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev0);
   // the split-step table goes to shared memory where it fits (FP64 4096-site
   // plans read it from global memory)
-  a2.kfac_smem = (!FAST && a.kfac != nullptr && Cfg::smem_bytes_split() <= size_t(maxsm)) ? 1 : 0;
+  a2.kfac_smem = ((SPLIT || !FAST) && a.kfac != nullptr && Cfg::smem_bytes_split() <= size_t(maxsm)) ? 1 : 0;
   const size_t smem = a2.kfac_smem ? Cfg::smem_bytes_split() : Cfg::smem_bytes();
   if (smem > size_t(maxsm)) {
     if (err) *err = "square kernel needs " + std::to_string(smem) + " B of shared memory (device max " +
                     std::to_string(maxsm) + ")";
     return false;
   }
-  auto fn = square_fft_kernel<R, P, CTA, FAST>;
+  auto fn = square_fft_kernel<R, P, CTA, FAST, SPLIT>;
   cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e != cudaSuccess) {
     cudaGetLastError();
@@ -60,7 +60,7 @@ bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo*
   const int64_t groups = (a.ntraj + Cfg::TPC - 1) / Cfg::TPC;
   const int grid = int(std::min<int64_t>(groups, int64_t(sms) * per_sm));
   if (info) {
-    info->name = FAST ? "square_fft_kernel<fast>" : "square_fft_kernel";
+    info->name = FAST ? (SPLIT ? "square_fft_kernel<fast,split>" : "square_fft_kernel<fast>") : "square_fft_kernel";
     info->cta = CTA;
     info->grid = grid;
     info->smem = smem;
@@ -79,12 +79,15 @@ bool square_launch_t(const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo*
 template <typename R>
 bool square_dispatch(int bx, int by, const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo* info,
                      std::string* err) {
-  // FP32 Euler runs with Philox noise and scalar U, F take the fast instantiation
-  const bool fast = sizeof(R) == 4 && a.noise_mode == 0 && a.iU == nullptr && a.iF == nullptr && a.kfac == nullptr;
-#define TWMC_SHAPE(BX, BY)                                                                          \
-  if (bx == BX && by == BY)                                                                         \
-    return fast ? square_launch_t<R, Plan_##BX##_##BY, sizeof(R) == 4>(a, nparams, s, info, err)   \
-                : square_launch_t<R, Plan_##BX##_##BY, false>(a, nparams, s, info, err);
+  // FP32 runs with Philox noise and scalar U, F take the fast instantiations
+  // (Euler, or the split step compiled in)
+  const bool fast = sizeof(R) == 4 && a.noise_mode == 0 && a.iU == nullptr && a.iF == nullptr;
+  const bool split = a.kfac != nullptr;
+#define TWMC_SHAPE(BX, BY)                                                                                   \
+  if (bx == BX && by == BY)                                                                                  \
+    return !fast    ? square_launch_t<R, Plan_##BX##_##BY, false>(a, nparams, s, info, err)                 \
+           : !split ? square_launch_t<R, Plan_##BX##_##BY, sizeof(R) == 4>(a, nparams, s, info, err)        \
+                    : square_launch_t<R, Plan_##BX##_##BY, sizeof(R) == 4, sizeof(R) == 4>(a, nparams, s, info, err);
   TWMC_SHAPE(0, 5) TWMC_SHAPE(0, 6) TWMC_SHAPE(0, 7) TWMC_SHAPE(0, 8) TWMC_SHAPE(0, 9) TWMC_SHAPE(0, 10)
   TWMC_SHAPE(0, 11) TWMC_SHAPE(0, 12) TWMC_SHAPE(4, 4) TWMC_SHAPE(5, 5) TWMC_SHAPE(6, 6)
 #undef TWMC_SHAPE

@@ -39,10 +39,11 @@ def test_split_step_differs_from_euler(built_lib, oracle):
     assert rel_err(a["final"], b["final"]) > 1e-6
 
 
-def test_split_step_philox(built_lib, oracle):
-    """Philox noise (the general FP32 instantiation takes the split step):
-    the oracle's split step fed the device's own Wiener normals."""
-    nx = ny = 32
+@pytest.mark.parametrize("nx,ny", [(32, 32), (64, 64), (1, 4096), (1, 256)])
+def test_split_step_philox(built_lib, oracle, nx, ny):
+    """Philox noise, scalar U and F, per-site omega (the fast instantiation
+    with the split step compiled in): the oracle's split step fed the
+    device's own Wiener normals."""
     n = nx * ny
     dt, fs, nfr = 0.002, 100, 2
     steps = fs * nfr
@@ -53,7 +54,7 @@ def test_split_step_philox(built_lib, oracle):
     res = sysd.run(tasks, frames=True, realizations=True)
     kernel = sysd.kernel_name
     sysd.close()
-    assert kernel == "square_fft_kernel", kernel
+    assert kernel == "square_fft_kernel<fast,split>", kernel
     for k in range(3):
         xi = twmc.debug_wiener(twmc.PREC_F32, 5 + k, 70 + k, steps, n)
         ref = oracle.base_run(nx, ny, 1.0, 1.0, dt, 0.0, steps * dt, fs, nfr + 1, True,
