@@ -103,6 +103,28 @@ def test_sim_archive_matches_c_abi(sim, tmp_path):
         assert ents[0]["t_start"] == 0.0 and ents[0]["t_end"] == res["t_final"][k]
 
 
+def test_sim_split_step_integrator(sim, tmp_path):
+    """The ini key integrator = "split" selects the exponential split step:
+    the archive equals the same run through the C ABI with
+    TWMC_INTEGRATOR_SPLIT and differs from the default (Euler) run."""
+    ini = tmp_path / "run.ini"
+    ini.write_text(INI + 'integrator = "split"\n')
+    out = tmp_path / "out"
+    run_sim(sim, ini, out)
+    seeds = mt19937(77, 6)
+    res = {}
+    for integ in (twmc.INTEGRATOR_SPLIT, twmc.INTEGRATOR_EULER):
+        s = twmc.System(nx=8, ny=8, J=1.0, gamma=1.0, dt=0.01, frame_steps=50,
+                        omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=0.2, F=1.5, beta_init_sigma=0.5,
+                        integrator=integ)
+        res[integ] = s.run(s.make_tasks(6, t_start=0.0, t_end=2.0, seeds=seeds, id0=1), frames=True)
+        s.close()
+    for k in range(6):
+        fr, _, _ = pr.read_trajectory(out / "data", k + 1)
+        assert np.array_equal(fr, res[twmc.INTEGRATOR_SPLIT]["frames"][k])
+        assert not np.allclose(fr[-1], res[twmc.INTEGRATOR_EULER]["frames"][k][-1], rtol=1e-6, atol=0)
+
+
 def test_sim_resume_appends_continuations(sim, tmp_path):
     ini = tmp_path / "run.ini"
     ini.write_text(INI)
