@@ -108,13 +108,14 @@ def test_sim_split_step_integrator(sim, tmp_path):
     the archive equals the same run through the C ABI with
     TWMC_INTEGRATOR_SPLIT and differs from the default (Euler) run."""
     ini = tmp_path / "run.ini"
-    ini.write_text(INI + 'integrator = "split"\n')
+    # 16 x 16: the split step needs a lattice the FFT kernel has a plan for
+    ini.write_text(INI.replace("nx = 8", "nx = 16").replace("ny = 8", "ny = 16") + 'integrator = "split"\n')
     out = tmp_path / "out"
     run_sim(sim, ini, out)
     seeds = mt19937(77, 6)
     res = {}
     for integ in (twmc.INTEGRATOR_SPLIT, twmc.INTEGRATOR_EULER):
-        s = twmc.System(nx=8, ny=8, J=1.0, gamma=1.0, dt=0.01, frame_steps=50,
+        s = twmc.System(nx=16, ny=16, J=1.0, gamma=1.0, dt=0.01, frame_steps=50,
                         omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=0.2, F=1.5, beta_init_sigma=0.5,
                         integrator=integ)
         res[integ] = s.run(s.make_tasks(6, t_start=0.0, t_end=2.0, seeds=seeds, id0=1), frames=True)
