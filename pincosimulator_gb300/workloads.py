@@ -36,10 +36,11 @@ DT = 0.002
 FRAME_STEPS = 250
 
 
-def square(nx, ny, hop=twmc.HOP_FFT, precision=twmc.PREC_F32, n_moment_blocks=32):
+def square(nx, ny, hop=twmc.HOP_FFT, precision=twmc.PREC_F32, n_moment_blocks=32, integrator=twmc.INTEGRATOR_EULER):
     return twmc.System(nx=nx, ny=ny, J=1.0, gamma=1.0, dt=DT, frame_steps=FRAME_STEPS,
                        omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=0.2, F=2.0, beta_init=0.0,
-                       beta_init_sigma=0.5, precision=precision, hop=hop, n_moment_blocks=n_moment_blocks)
+                       beta_init_sigma=0.5, precision=precision, hop=hop, n_moment_blocks=n_moment_blocks,
+                       integrator=integrator)
 
 
 def lieb(ncell=256):
@@ -122,6 +123,8 @@ def main(argv=None):
     ap.add_argument("--ntraj", type=int, default=2048)
     ap.add_argument("--frames", type=int, default=1)
     ap.add_argument("--hop", choices=["fft", "stencil"], default="stencil")
+    ap.add_argument("--integrator", choices=["euler", "split"], default="euler",
+                    help="square64 / square128 with --hop fft: the step's integrator")
     args = ap.parse_args(argv)
     if args.workload == "batch256":
         el, sites, plans = time_hbatch(batch_points(traj_scale=args.traj_scale), args.frames)
@@ -137,7 +140,8 @@ def main(argv=None):
         el, finite = time_run(sysd, args.ntraj, args.frames, save=True)
     else:
         L = 64 if args.workload == "square64" else 128
-        sysd = square(L, L, hop=twmc.HOP_STENCIL if args.hop == "stencil" else twmc.HOP_FFT)
+        sysd = square(L, L, hop=twmc.HOP_STENCIL if args.hop == "stencil" else twmc.HOP_FFT,
+                      integrator=twmc.INTEGRATOR_SPLIT if args.integrator == "split" else twmc.INTEGRATOR_EULER)
         el, finite = time_batch(sysd, args.ntraj, args.frames), True
     line = {"workload": args.workload, "ntraj": args.ntraj, "frames": args.frames, "kernel": sysd.kernel_name,
             "seconds": el, "site_updates_per_s": sysd.n_sites * args.ntraj * args.frames * sysd.desc.frame_steps / el,
