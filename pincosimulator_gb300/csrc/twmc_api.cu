@@ -94,6 +94,10 @@ struct twmc_handle {
   bool timedep = false;
   bool thermo = false;     // work / area accumulators (TWMCThermoSolver)
   int integrator = TWMC_INTEGRATOR_EULER;
+  // every trajectory's per-site rsl has the real part par_scalar[0][0]
+  // (square lattice: Im omega uniform over the base, the disorder and any
+  // given realisations); set by the batch initialisation
+  bool rsl_re_uniform = false;
   DevBuf d_work, d_area;
   DevBuf d_wide;           // FP32 -> FP64 download staging (bounded chunk)
   // final-field pipeline of twmc_run: the last steps run in kFinalChunks
@@ -450,6 +454,7 @@ int advance(twmc_handle* h, int64_t n, bool want_nk, int64_t t0 = 0, int64_t t1 
   a.tw = h->d_tw.p;
   a.ktab = h->d_ktab.p;
   a.kfac = h->integrator == TWMC_INTEGRATOR_SPLIT ? h->d_kfac.p : nullptr;
+  a.rsl_re_uniform = h->rsl_re_uniform ? 1 : 0;
   a.nsites = h->nsites;
   a.nx = h->lattice == TWMC_LATTICE_SQUARE ? h->nx : 1;
   a.ny = h->lattice == TWMC_LATTICE_SQUARE ? h->ny : h->nsites;
@@ -568,6 +573,24 @@ int batch_init(twmc_handle* h, const twmc_task_desc* tasks, size_t n) {
     }
     if (!upload_raw(&h->d_given, g.data(), g.size())) return fail(h, TWMC_ERR_NOMEM, "initial field upload");
     ia.given = h->d_given.as<double>();
+  }
+  // Real part of rsl = Im(omega) - gamma/2 the same at every site of every
+  // trajectory: Im of the base uniform, no imaginary disorder amplitude, and
+  // given realisations with that imaginary part (square lattice).
+  {
+    bool uni = h->lattice == TWMC_LATTICE_SQUARE;
+    const Matrix& mo = h->m_omega;
+    const double im0 = mo.base.empty() ? 0.0 : mo.base[0].imag();
+    for (const cd& v : mo.base) uni = uni && v.imag() == im0;
+    if (mo.kind != TWMC_DISORDER_NONE)
+      for (const cd& v : mo.amp) uni = uni && v.imag() == 0.0;
+    if (tasks[0].omega_realization)
+      for (size_t i = 0; i < n && uni; ++i) {
+        const double* w = tasks[i].omega_realization;
+        if (!w) { uni = false; break; }  // rejected below: all tasks or none
+        for (int64_t j = 0; j < N && uni; ++j) uni = w[2 * j + 1] == im0;
+      }
+    h->rsl_re_uniform = uni;
   }
   // matrices: 0 = U, 1 = omega/E, 2 = F ; per-site parameter buffers: rsl <- omega, iU <- U, iF <- F
   const Matrix* mats[3] = {&h->m_U, &h->m_omega, &h->m_F};

@@ -56,6 +56,8 @@ struct StepArgs {
   const void* kfac;       // exponential split step: [N] complex R, (exp(-i 2J c_k dt) - 1) / N at each
                           // position of the forward plan's output; NULL = the Euler step
   int kfac_smem;          // split step: 1 = table copied to shared memory, 0 = read from global (L2)
+  int rsl_re_uniform;     // per-site rsl with the same real part (-gamma/2 + Im omega) everywhere, equal
+                          // to rsl_s[0]: the fast FFT kernel then reads the imaginary parts only
   // ell kernel
   int tpt;                // threads per trajectory
   int64_t nsites;         // N
@@ -327,6 +329,13 @@ template <class P> struct TwSlots {
   }
   static constexpr int total() { return base(P::npass, 0); }
 };
+
+// Plans whose single-system FP32 kernel holds the thread-dependent twiddles
+// in registers for the whole launch (chains of 1024 sites and more).
+template <class P>
+constexpr bool plan_reg_twiddles() {
+  return P::bx == 0 && P::nbits >= 10 && TwSlots<P>::total() > 0;
+}
 
 // Padded position of the CTA-flat element index: one pad slot after every 16
 // elements. For indices with disjoint bits pad(a | b) = pad(a) + pad(b), so
@@ -834,7 +843,13 @@ struct SquareGroup {
     // conflicts on a 3072-entry table); measured on GB300: 1x4096 0.95e11 ->
     // 1.74e11 site-updates/s, 1x1024 1.90e11 -> 2.05e11, while 64x64 (-11 %),
     // 32x32 (-3 %) and 1x256 (-5 %) lost to the extra register pressure.
-    constexpr bool HT = REG_SMALL && sizeof(R) == 4 && P::bx == 0 && P::nbits >= 10 && TwSlots<P>::total() > 0;
+    constexpr bool HT = REG_SMALL && sizeof(R) == 4 && plan_reg_twiddles<P>();
+    // RE_RSL: the fast single-system kernel (launched only when the per-site
+    // rsl share one real part, rsl_re_uniform) keeps 16 per-site values
+    // instead of 32 for the launch; measured on GB300: 64x64 2.19e11 ->
+    // 2.27e11, 32x32 2.30e11 -> 2.35e11, 16x16 3.36e11 -> 3.48e11
+    // site-updates/s, while the register-twiddle chains lost 4 %.
+    constexpr bool RE_RSL = FAST && REG_SMALL && sizeof(R) == 4 && !HT;
     T twr[HT ? TwSlots<P>::total() : 1];
     if constexpr (HT) load_twiddle_set<P>(twr, tw0, tw1, pos_thr);
 
@@ -914,7 +929,15 @@ struct SquareGroup {
         {
           const int plo = pos_thr[0] | I::pos_reg(0, s_lo);
           const int phi = pos_thr[0] | I::pos_reg(0, s_hi);
-          if (has_rsl) { r_lo = __ldg(g_rsl + plo); r_hi = __ldg(g_rsl + phi); }
+          if (has_rsl) {
+            if constexpr (RE_RSL) {
+              r_lo = cmake<T>(rsl_s.x, __ldg(&g_rsl[plo].y));
+              r_hi = cmake<T>(rsl_s.x, __ldg(&g_rsl[phi].y));
+            } else {
+              r_lo = __ldg(g_rsl + plo);
+              r_hi = __ldg(g_rsl + phi);
+            }
+          }
           if (has_iU) { u_lo = __ldg(g_iU + plo); u_hi = __ldg(g_iU + phi); }
           if (has_iF) { f_lo = __ldg(g_iF + plo); f_hi = __ldg(g_iF + phi); }
         }

@@ -81,11 +81,15 @@ bool square_dispatch(int bx, int by, const StepArgs& a, int nparams, cudaStream_
                      std::string* err) {
   // FP32 runs with Philox noise and scalar U, F take the fast instantiations
   // (Euler, or the split step compiled in)
+  // (per-site rsl: with one real part everywhere, except on the plans that
+  // keep their twiddles in registers, which read the whole values)
   const bool fast = sizeof(R) == 4 && a.noise_mode == 0 && a.iU == nullptr && a.iF == nullptr;
   const bool split = a.kfac != nullptr;
+  const bool rsl_ok = a.rsl == nullptr || a.rsl_re_uniform;
 #define TWMC_SHAPE(BX, BY)                                                                                   \
   if (bx == BX && by == BY)                                                                                  \
-    return !fast    ? square_launch_t<R, Plan_##BX##_##BY, false>(a, nparams, s, info, err)                 \
+    return !(fast && (rsl_ok || plan_reg_twiddles<Plan_##BX##_##BY>()))                                     \
+               ? square_launch_t<R, Plan_##BX##_##BY, false>(a, nparams, s, info, err)                      \
            : !split ? square_launch_t<R, Plan_##BX##_##BY, sizeof(R) == 4>(a, nparams, s, info, err)        \
                     : square_launch_t<R, Plan_##BX##_##BY, sizeof(R) == 4, sizeof(R) == 4>(a, nparams, s, info, err);
   TWMC_SHAPE(0, 5) TWMC_SHAPE(0, 6) TWMC_SHAPE(0, 7) TWMC_SHAPE(0, 8) TWMC_SHAPE(0, 9) TWMC_SHAPE(0, 10)
