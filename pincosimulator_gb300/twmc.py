@@ -275,12 +275,20 @@ class System:
 
     # -- tasks -----------------------------------------------------------
     def make_tasks(self, n: int, *, t_start=0.0, t_end=1.0, seed0=1234, id0=1, store_initial=True,
-                   ic=IC_SETTINGS, init_field=None, seeds: Optional[Sequence[int]] = None):
+                   ic=IC_SETTINGS, init_field=None, seeds: Optional[Sequence[int]] = None,
+                   realizations: Optional[dict] = None):
+        """n task descriptors. `realizations` may give the disorder
+        realisations per task ({"U" | "omega" | "F": (n, n_sites) complex}),
+        as a continuation run passes the stored datasets."""
         tasks = (TaskDesc * n)()
         keep = []
         if init_field is not None:
             f = np.ascontiguousarray(np.asarray(init_field, dtype=np.complex128).reshape(n, self.n_sites))
             keep.append(f)
+        given = {}
+        for name, arr in (realizations or {}).items():
+            given[name] = np.ascontiguousarray(np.asarray(arr, dtype=np.complex128).reshape(n, self.n_sites))
+            keep.append(given[name])
         for i in range(n):
             t = tasks[i]
             t.id = id0 + i
@@ -290,6 +298,8 @@ class System:
             t.store_initial = int(bool(store_initial))
             if init_field is not None:
                 t.init_field = f[i].ctypes.data
+            for name, arr in given.items():
+                setattr(t, name + "_realization", arr[i].ctypes.data)
         self._keep.append(keep)
         return tasks
 

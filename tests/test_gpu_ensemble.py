@@ -168,3 +168,32 @@ def test_long_run_against_oracle_ensemble(built_lib, oracle, long_runs):
     for k in ("n", "g2", "n_site_avg"):
         assert c[k]["max_abs_z"] < 5.0, (k, c[k])
         assert c[k]["mean_z2"] < 1.6, (k, c[k])
+
+
+@pytest.mark.parametrize("im", [0.0, "varying"])
+def test_given_omega_realisations_pick_the_kernel(built_lib, oracle, im):
+    """Continuation-style runs with given omega realisations: a realisation
+    whose imaginary part is uniform keeps the fast kernel (it reads only the
+    imaginary parts of rsl), one with a varying imaginary part takes the
+    general kernel; both equal the oracle fed the device's normals."""
+    nx = ny = 32
+    n = nx * ny
+    ntraj, fs, nfr = 2, 100, 2
+    steps = fs * nfr
+    rng = np.random.default_rng(21)
+    om = -0.5 + 0.2 * rng.normal(size=(ntraj, n)) + 0j
+    if im == "varying":
+        om = om + 0.03j * rng.normal(size=(ntraj, n))
+    sysd = twmc.System(nx=nx, ny=ny, J=J, gamma=GAMMA, dt=DT, frame_steps=fs,
+                       omega=twmc.Noisy(-0.5, twmc.DISORDER_GAUSSIAN, 0.2), U=U, F=F, beta_init_sigma=0.5)
+    tasks = sysd.make_tasks(ntraj, t_end=steps * DT, seed0=33, id0=3, realizations={"omega": om})
+    res = sysd.run(tasks, frames=True, realizations=True)
+    kernel = sysd.kernel_name
+    sysd.close()
+    assert kernel == ("square_fft_kernel" if im == "varying" else "square_fft_kernel<fast>"), kernel
+    assert np.array_equal(res["omega_realization"], om)
+    for k in range(ntraj):
+        xi = twmc.debug_wiener(twmc.PREC_F32, 33 + k, 3 + k, steps, n)
+        ref = oracle.base_run(nx, ny, J, GAMMA, DT, 0.0, steps * DT, fs, nfr + 1, True, om[k], U, F,
+                              res["frames"][k, 0], xi=xi)
+        assert rel_err(res["final"][k], ref["final"]) < 1e-5
