@@ -857,12 +857,13 @@ struct SquareGroup {
     // carried from the local update (which also stores it to the slices),
     // instead of reloaded from the slices every step; measured on GB300:
     // 64x64 0.4 % faster, while the chains with their twiddles in registers
-    // (HT) lost 6 % to the longer register lifetimes. Those chains take the
-    // multiply-add form of the local update (local_update_fused<true>):
-    // 1x4096 1.77e11 -> 1.79e11, 1x1024 2.05e11 -> 2.09e11 site-updates/s,
-    // while 64x64 (2.19e11 -> 2.14e11), 32x32 and 1x256 were faster
-    // without it.
+    // (HT) lost 6 % to the longer register lifetimes. LU_MADD: the
+    // multiply-add form of the local update (local_update_fused<true>) on
+    // every plan but 64x64: 1x4096 1.77e11 -> 1.79e11, 1x1024 2.05e11 ->
+    // 2.09e11, 32x32 2.34e11 -> 2.47e11 site-updates/s, while 64x64 measured
+    // 1 % faster without it.
     constexpr bool CARRY = !HT;
+    constexpr bool LU_MADD = HT || P::nbits < 12;
     T x[E];
     static_for<E>([&](auto S) { x[decltype(S)::value] = bget(S); });
     for (int64_t step = 0; step < a.nsteps; ++step) {
@@ -955,8 +956,8 @@ struct SquareGroup {
             n_hi = local_update(b_hi, zero, r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi);
           }
         } else if constexpr (sizeof(R) == 4) {  // dt is folded into the k-space table
-          n_lo = local_update_fused<HT>(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo);
-          n_hi = local_update_fused<HT>(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi);
+          n_lo = local_update_fused<LU_MADD>(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo);
+          n_hi = local_update_fused<LU_MADD>(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi);
         } else {
           n_lo = local_update(bget(SL), x[s_lo], r_lo, u_lo, f_lo, dt, Wiener<R>::scale(dt4), xi_lo);
           n_hi = local_update(bget(SH), x[s_hi], r_hi, u_hi, f_hi, dt, Wiener<R>::scale(dt4), xi_hi);
