@@ -68,6 +68,12 @@ TWMCSystemData::TWMCSystemData(const Settings& s) {
   precision = s.getString("precision", "f32");
   hop = s.getString("hop", "fft");
   integrator = s.getString("integrator", "euler");
+  if (integrator != "euler" && integrator != "split")
+    throw std::runtime_error("integrator must be \"euler\" or \"split\", not \"" + integrator + "\"");
+  if (hop != "fft" && hop != "stencil")
+    throw std::runtime_error("hop must be \"fft\" or \"stencil\", not \"" + hop + "\"");
+  if (precision != "f32" && precision != "f64")
+    throw std::runtime_error("precision must be \"f32\" or \"f64\", not \"" + precision + "\"");
 }
 
 size_t TWMCSystemData::ComputeNFrames(double ts, double te) const {

@@ -61,6 +61,7 @@ void describe(const Settings& s, const TWMCSystemData& d) {
     << ",\"nFramesTot\":" << d.nFramesTot << ",\"n_dt\":" << d.n_dt << ",\"n_traj\":" << s.getSize("n_traj")
     << ",\"seed\":" << s.GlobalSeed() << ",\"manager\":\"" << s.getString("Manager") << "\""
     << ",\"output\":\"" << s.GetOutputFolder() << "\""
+    << ",\"precision\":\"" << d.precision << "\",\"hop\":\"" << d.hop << "\",\"integrator\":\"" << d.integrator << "\""
     << ",\"U\":" << json_matrix(d.U) << ",\"F\":" << json_matrix(d.F) << ",\"omega\":" << json_matrix(d.omega)
     << ",\"E\":" << json_matrix(d.E) << ",\"beta_init\":" << json_matrix(d.beta_init)
     << ",\"beta_init_sigma\":" << json_matrix(d.beta_init_sigma) << ",\"stored_times\":[";

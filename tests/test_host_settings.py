@@ -138,3 +138,19 @@ def test_folder_input_reads_sim_ini(sim, tmp_path):
     assert r.returncode == 0, r.stderr
     d = json.loads(r.stdout)
     assert d["output"] == str(tmp_path) and np.allclose(cvec(d["U"]["base"]), 0.3)
+
+
+def test_engine_options(sim, tmp_path):
+    """The engine's own keys (absent from the reference's inputs): precision,
+    hop and integrator, from the .ini and as command-line overrides; an
+    unknown value is an error."""
+    d = describe(sim, write(tmp_path, BASE))
+    assert (d["precision"], d["hop"], d["integrator"]) == ("f32", "fft", "euler")
+    ini = write(tmp_path, BASE + 'integrator = "split"\nprecision = "f64"\n')
+    d = describe(sim, ini)
+    assert (d["precision"], d["hop"], d["integrator"]) == ("f64", "fft", "split")
+    d = describe(sim, ini, "hop", '"stencil"', "integrator", '"euler"')  # overrides are TOML values
+    assert (d["hop"], d["integrator"]) == ("stencil", "euler")
+    for key, val in (("integrator", '"rk4"'), ("hop", '"dense"'), ("precision", '"f16"')):
+        r = subprocess.run([sim, "--describe", "-i", str(ini), key, val], capture_output=True, text=True)
+        assert r.returncode != 0 and key in r.stderr, (key, r.stderr)
