@@ -80,9 +80,9 @@ template <typename R>
 bool square_dispatch(int bx, int by, const StepArgs& a, int nparams, cudaStream_t s, LaunchInfo* info,
                      std::string* err) {
   // FP32 runs with Philox noise and scalar U, F take the fast instantiations
-  // (Euler, or the split step compiled in)
-  // (per-site rsl: with one real part everywhere, except on the plans that
-  // keep their twiddles in registers, which read the whole values)
+  // (Euler, or the split step compiled in); a per-site rsl must have one real
+  // part everywhere, except on the plans that keep their twiddles in
+  // registers, whose fast kernel reads the whole values
   const bool fast = sizeof(R) == 4 && a.noise_mode == 0 && a.iU == nullptr && a.iF == nullptr;
   const bool split = a.kfac != nullptr;
   const bool rsl_ok = a.rsl == nullptr || a.rsl_re_uniform;
